@@ -1,0 +1,331 @@
+#!/usr/bin/env python3
+"""Benchmark: BVH closest-hit traversal throughput (Mrays/s) on the 1,310,720-triangle
+displaced icosphere with 2^23 rays, on one GB300 per rank.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one closest-hit pass (ckr_trace_closest) over the 2^23-ray batch
+(4,194,304 primary rays of a 2048x2048 pinhole camera at distance 3 + 4,194,304
+incoherent rays, origins uniform in the mesh AABB, directions uniform, seed 7), inputs
+resident in HBM.  `e2e` is the same metric through ckr_trace_closest_host with pinned
+host buffers (ray upload and hit download inside the timed region).  Rank 0 prints one
+JSON line.  Under torchrun each rank traces its own copy of the batch (weak scaling, no
+data-path collective).  `--impl reference` times the reference's CPU traversal
+(BvhAccel::intersectT) on the host cores: its FP64 restatement in oracle/ (the reference
+binary itself cannot run on this host), each step a bounded sample of the batch.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mrays/s at 1.3M tris; relMSE at equal time, learned vs plain MIS, 1 GB300"
+UNIT = "Mrays/s"
+NRAYS_HALF = 4194304
+WORKLOAD = ("bvh-traversal: displaced icosphere (8 subdivisions, 1,310,720 tris, value-noise amp 0.05, "
+            "6 octaves), 2^23 rays = 4,194,304 primary (2048x2048 pinhole, distance 3, 40 deg) + "
+            "4,194,304 incoherent (uniform in AABB, uniform directions, seed 7); closest-hit")
+
+
+def make_workload():
+    from chakumrender_gb300 import ckr
+
+    tri = ckr.icosphere(8, 0.05, 6, 1)
+    lo, hi = tri.reshape(-1, 3).min(0), tri.reshape(-1, 3).max(0)
+    primary = ckr.rays_pinhole([0, 0, 3], [0, 0, 0], [0, 1, 0], 40.0, 2048, 2048)
+    incoh = ckr.rays_incoherent(lo, hi, 7, NRAYS_HALF, 0.05, 2.0)
+    closest = np.concatenate([primary, incoh])
+    anyhit = closest.copy()
+    closest[:, 7] = 1e30
+    return tri, closest, anyhit
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profile():
+    """Per-launch DRAM bytes of the closest-hit kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "trace_closest_icosphere_1310720.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.strip().startswith("dram_bytes_per_launch"):
+            try:
+                return float(line.split("=")[1].split()[0])
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def run_reference(args, rank, world):
+    """CPU arm: the reference's traversal on the host cores (FP64 restatement of
+    BvhAccel::intersectT over the reference's midpoint BVH)."""
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from chakumrender_gb300 import build
+
+    build.build_library()
+    build.build_oracle()
+    import oracle as O
+
+    tri, closest, _ = make_workload()
+    cores = os.cpu_count() or 1
+    sample_n = 1 << 18  # rays per step: a stride sample over both halves of the batch
+    stride = len(closest) // sample_n
+    t0 = time.perf_counter()
+    ob = O.OracleBvh(tri)
+    build_s = time.perf_counter() - t0
+    times = []
+    for k in range(args.warmup + args.steps):
+        rays = np.ascontiguousarray(closest[(k % stride)::stride][:sample_n])
+        t0 = time.perf_counter()
+        ob.closest(rays, threads=cores)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+    mrays = sample_n * len(times) / sum(times) / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": round(mrays, 4), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample_rays_per_step": sample_n, "bvh_build_s": round(build_s, 3)},
+            "cpu_baseline": {"value": round(mrays, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{sample_n} rays per step (stride-{stride} sample of the 2^23-ray batch)"},
+            "e2e": {"value": round(mrays, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(tri, closest):
+    """The oracle port of the reference traversal on the host cores, bounded sample."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from chakumrender_gb300 import build
+
+    build.build_oracle()
+    import oracle as O
+
+    cores = os.cpu_count() or 1
+    ob = O.OracleBvh(tri)
+    n = 1 << 20
+    stride = len(closest) // n
+    rays = np.ascontiguousarray(closest[::stride][:n])
+    t0 = time.perf_counter()
+    _, _, nv, nt = ob.closest(rays, threads=cores, counts=True)
+    dt = time.perf_counter() - t0
+    half = n // 2
+    return ({"value": round(n / dt / 1e6, 4), "unit": UNIT, "cores": cores, "kind": "port",
+             "sample": f"{n} rays (stride-{stride} sample of the 2^23-ray batch), FP64 restatement of "
+                       f"BvhAccel::intersectT over the reference's midpoint BVH"},
+            {"primary": [float(nv[:half].mean()), float(nt[:half].mean())],
+             "incoherent": [float(nv[half:].mean()), float(nt[half:].mean())]})
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--leaf", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from chakumrender_gb300 import build
+
+    build.build_library()
+    from chakumrender_gb300 import ckr
+
+    tri, closest, anyhit = make_workload()
+    scene = ckr.Scene(tri, max_leaf_size=args.leaf)
+    info = scene.info()
+    n = len(closest)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    d_rays = torch.from_numpy(closest).cuda()
+    d_any = torch.from_numpy(anyhit).cuda()
+    ids = torch.empty(n, dtype=torch.int32, device="cuda")
+    ts = torch.empty(n, dtype=torch.float32, device="cuda")
+    occ = torch.empty(n, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        scene.trace_closest(d_rays.data_ptr(), n, ids.data_ptr(), ts.data_ptr(), sh)
+    torch.cuda.synchronize()
+    if scene.check_device(sh) != 0:
+        raise SystemExit("device status error during warm-up")
+
+    # Device-resident throughput: K steps, each bracketed by CUDA events on the launch stream.
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        barrier()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            ev[k][0].record(stream)
+            scene.trace_closest(d_rays.data_ptr(), n, ids.data_ptr(), ts.data_ptr(), sh)
+            ev[k][1].record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+    clocks = clk.summary()
+    kernel_ms = [a.elapsed_time(b) for a, b in ev]
+    step_ms = sum(kernel_ms) / len(kernel_ms)
+    t_max = torch.tensor([wall], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+    total_rays = n * args.steps * world
+    value = total_rays / float(t_max.item()) / 1e6
+
+    # Any-hit pass (reported alongside).
+    for _ in range(2):
+        scene.trace_any(d_any.data_ptr(), n, occ.data_ptr(), sh)
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a0.record(stream)
+    for _ in range(args.steps):
+        scene.trace_any(d_any.data_ptr(), n, occ.data_ptr(), sh)
+    a1.record(stream)
+    torch.cuda.synchronize()
+    any_mrays = n * args.steps / (a0.elapsed_time(a1) / 1e3) / 1e6
+
+    # End to end through the host-buffer C ABI (pinned buffers, copies inside the timed region).
+    h_rays = torch.from_numpy(closest).pin_memory()
+    h_ids = torch.empty(n, dtype=torch.int32).pin_memory()
+    h_t = torch.empty(n, dtype=torch.float32).pin_memory()
+    L = ckr.lib()
+    for _ in range(2):
+        ckr.check(L.ckr_trace_closest_host(scene.handle, h_rays.data_ptr(), n, h_ids.data_ptr(), h_t.data_ptr(), sh),
+                  "e2e warm-up")
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ckr.check(L.ckr_trace_closest_host(scene.handle, h_rays.data_ptr(), n, h_ids.data_ptr(), h_t.data_ptr(), sh),
+                  "e2e")
+    barrier()
+    e2e_wall = torch.tensor([time.perf_counter() - t0], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(e2e_wall, op=dist.ReduceOp.MAX)
+    e2e = n * args.steps * world / float(e2e_wall.item()) / 1e6
+
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+
+    # Roofline: algorithmic bytes per ray from the replayed box/triangle counts.
+    sample = np.ascontiguousarray(closest[::16])
+    mean_boxes, mean_tris = scene.stats(sample)
+    bytes_per_ray = 32 + 8 + 32 * mean_boxes + 36 * mean_tris
+    achieved = n * bytes_per_ray / (step_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = traffic_from_profile()
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "rays_per_step": n, "triangles": int(info.ntri),
+                   "bvh": f"binned SAH, leaf<={args.leaf}, {info.nnodes} interior nodes, depth {info.max_depth}",
+                   "bvh_build_ms": round(info.build_ms, 1), "l2": "inputs larger than L2 (rays 256 MiB), no flush",
+                   "parallelism": f"replica x{world}"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
+                     "bytes_per_ray": round(bytes_per_ray, 1), "mean_boxes": round(mean_boxes, 2),
+                     "mean_tris": round(mean_tris, 3)},
+        "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 8},
+        "gpu_launches": args.steps,
+        "any_hit_mrays": round(any_mrays, 3),
+        "kernel_ms_min_max": [round(min(kernel_ms), 4), round(max(kernel_ms), 4)],
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        cb, ref_counts = cpu_baseline(tri, closest)
+        line["cpu_baseline"] = cb
+        line["roofline"]["reference_bvh_counts"] = ref_counts
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

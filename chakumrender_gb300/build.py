@@ -1,0 +1,100 @@
+"""Builds libckr.so in-tree: CUDA sources with nvcc for sm_103a, host C++ with g++.
+
+Objects go to chakumrender_gb300/_build/, the library to chakumrender_gb300/libckr.so.
+Translation units compile in parallel; an object is rebuilt when its source or any
+header under csrc/ or include/ is newer.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB = PKG / "libckr.so"
+CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
+
+
+def _nvcc() -> str:
+    p = CUDA_HOME / "bin" / "nvcc"
+    return str(p) if p.exists() else (shutil.which("nvcc") or "nvcc")
+
+
+def _headers_mtime() -> float:
+    hs = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
+    return max((h.stat().st_mtime for h in hs), default=0.0)
+
+
+def _compile_cmd(src: Path, obj: Path) -> list[str]:
+    inc = ["-I", str(ROOT / "include"), "-I", str(CSRC)]
+    if src.suffix == ".cu":
+        return [_nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "--expt-relaxed-constexpr",
+                "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-warn-spills",
+                *inc, "-c", str(src), "-o", str(obj)]
+    return ["g++", *HOST_FLAGS, *inc, "-I", str(CUDA_HOME / "include"), "-c", str(src), "-o", str(obj)]
+
+
+def build_library(verbose: bool = False, jobs: int | None = None) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    srcs = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
+    hdr_t = _headers_mtime()
+    todo = []
+    for s in srcs:
+        obj = BUILD / (s.name + ".o")
+        if not obj.exists() or obj.stat().st_mtime < max(s.stat().st_mtime, hdr_t):
+            todo.append((s, obj))
+
+    def run(job):
+        s, obj = job
+        cmd = _compile_cmd(s, obj)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        if verbose and (r.stdout.strip() or r.stderr.strip()):
+            print(r.stdout + r.stderr, file=sys.stderr)
+        return s.name
+
+    with ThreadPoolExecutor(max_workers=jobs or min(16, os.cpu_count() or 4)) as ex:
+        for name in ex.map(run, todo):
+            if verbose:
+                print(f"[build] compiled {name}", file=sys.stderr)
+    objs = [str(BUILD / (s.name + ".o")) for s in srcs]
+    newest = max(Path(o).stat().st_mtime for o in objs)
+    if todo or not LIB.exists() or LIB.stat().st_mtime < newest:
+        tmp = LIB.with_suffix(".so.tmp")
+        cmd = [_nvcc(), *ARCH, "-shared", "-o", str(tmp), *objs, "-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, LIB)
+        if verbose:
+            print(f"[build] linked {LIB}", file=sys.stderr)
+    return LIB
+
+
+def build_oracle(verbose: bool = False) -> None:
+    """Builds oracle/liboracle.so, and oracle/_ref/ where the reference sources exist."""
+    odir = ROOT / "oracle"
+    targets = ["all"]
+    ref = Path(os.environ.get("CKR_REFERENCE", "/root/reference"))
+    if (ref / "src" / "bvhAccel.cpp").exists():
+        targets.append("ref")
+    cmd = ["make", "-s", "-C", str(odir), f"-j{min(16, os.cpu_count() or 4)}", f"REF={ref}", *targets]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if verbose:
+        print(f"[build] oracle targets {targets}", file=sys.stderr)
+
+
+if __name__ == "__main__":
+    build_library(verbose=True)
+    build_oracle(verbose=True)

@@ -1,0 +1,296 @@
+// trace.cu — scene upload and the closest-hit / any-hit traversal kernels.
+//
+// One thread per ray; a persistent grid (a multiple of the SM count) strides
+// over the ray list.  Each thread keeps its traversal stack in shared memory,
+// laid out level-major ([level][thread]) so stack traffic is bank-conflict
+// free.  BVH nodes (64 B: both child boxes + links) and triangles (48 B) are
+// read with 16-byte read-only loads.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "bvh_build.h"
+#include "ckr_internal.h"
+#include "trace_device.cuh"
+
+struct ckr_scene {
+  int device = 0;
+  ckr::DevBuf<float4> nodes, tris, spheres;
+  ckr::DevBuf<int> status;
+  int32_t root = ckr::kDone;
+  uint32_t ntri = 0, nsph = 0, nnodes = 0, nleaves = 0, max_depth = 0;
+  double build_ms = 0.0;
+  std::vector<float> host_nodes, host_tris;  // kept for the host statistics replay
+  std::vector<float> host_spheres;
+  // Staging for the host-buffer entry points.
+  std::mutex host_mu;
+  ckr::DevBuf<ckr_ray> st_rays;
+  ckr::DevBuf<uint32_t> st_id;
+  ckr::DevBuf<float> st_t;
+  ckr::DevBuf<uint8_t> st_occ;
+  cudaStream_t pipe[2] = {nullptr, nullptr};
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+namespace ckr {
+
+SceneView view_of(const ckr_scene *s) {
+  SceneView v;
+  v.nodes = s->nodes.ptr;
+  v.tris = s->tris.ptr;
+  v.spheres = s->spheres.ptr;
+  v.root = s->root;
+  v.nsph = s->nsph;
+  v.status = s->status.ptr;
+  return v;
+}
+
+uint32_t stack_depth_of(const ckr_scene *s) { return std::max<uint32_t>(1, s->max_depth); }
+
+namespace {
+
+constexpr int kTPB = 128;
+
+template <bool ANY>
+__global__ void __launch_bounds__(kTPB) k_trace(SceneView s, const float4 *__restrict__ rays, uint32_t n,
+                                                uint32_t *__restrict__ hit_id, float *__restrict__ hit_t,
+                                                uint8_t *__restrict__ occluded, int depth) {
+  extern __shared__ int32_t smem_stack[];
+  int32_t *stack = smem_stack + threadIdx.x;
+  for (uint32_t i = blockIdx.x * kTPB + threadIdx.x; i < n; i += gridDim.x * kTPB) {
+    float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
+    RayPre r = make_ray(a, b);
+    float tbest = b.w;
+    uint32_t id = trace_ray<ANY>(s, r, tbest, stack, kTPB, depth);
+    if (ANY) {
+      occluded[i] = id != kMiss ? 1 : 0;
+    } else {
+      hit_id[i] = id;
+      hit_t[i] = tbest;
+    }
+  }
+}
+
+struct LaunchShape {
+  int grid;
+  size_t smem;
+};
+
+template <bool ANY>
+cudaError_t launch_shape(const ckr_scene *s, uint32_t n, LaunchShape &ls) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  ls.smem = (size_t)stack_depth_of(s) * kTPB * sizeof(int32_t);
+  if (ls.smem > 48 * 1024) {
+    e = cudaFuncSetAttribute(k_trace<ANY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls.smem);
+    if (e != cudaSuccess) return e;
+  }
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<ANY>, kTPB, ls.smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int want = (int)ceil_div(n, kTPB);
+  ls.grid = std::max(1, std::min(want, sms * per_sm));
+  return cudaSuccess;
+}
+
+template <bool ANY>
+int launch_trace(const ckr_scene *s, const ckr_ray *rays, uint32_t n, uint32_t *hit_id, float *hit_t,
+                 uint8_t *occluded, cudaStream_t stream) {
+  if (n == 0) return CKR_OK;
+  LaunchShape ls;
+  CKR_CUDA_TRY(launch_shape<ANY>(s, n, ls));
+  k_trace<ANY><<<ls.grid, kTPB, ls.smem, stream>>>(view_of(s), reinterpret_cast<const float4 *>(rays), n, hit_id,
+                                                   hit_t, occluded, (int)stack_depth_of(s));
+  CKR_CUDA_TRY(cudaGetLastError());
+  return CKR_OK;
+}
+
+bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+}  // namespace
+}  // namespace ckr
+
+using namespace ckr;
+
+extern "C" int ckr_scene_create(const float *tri9, uint32_t ntri, const float *sph4, uint32_t nsph,
+                                const ckr_build_params *params, ckr_scene **out) {
+  if (!out || (ntri && !tri9) || (nsph && !sph4)) return CKR_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return CKR_ERR_NO_DEVICE;
+  ckr_build_params p = params ? *params : ckr_build_params{0, 0, 0};
+  auto t0 = std::chrono::steady_clock::now();
+  FlatBvh bvh;
+  int st = build_bvh(tri9, ntri, p, bvh);
+  if (st != CKR_OK) return st;
+  auto t1 = std::chrono::steady_clock::now();
+  ckr_scene *s = new (std::nothrow) ckr_scene();
+  if (!s) return CKR_ERR_OUT_OF_MEMORY;
+  auto fail = [&](int code) {
+    delete s;
+    return code;
+  };
+  if (cudaGetDevice(&s->device) != cudaSuccess) return fail(CKR_ERR_CUDA);
+  s->ntri = ntri;
+  s->nsph = nsph;
+  s->root = bvh.root;
+  s->nnodes = bvh.nnodes;
+  s->nleaves = bvh.nleaves;
+  s->max_depth = bvh.max_depth;
+  s->build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  size_t nn = std::max<size_t>(1, bvh.nodes.size() / 4), nt = std::max<size_t>(1, bvh.tris.size() / 4);
+  if (s->nodes.reserve(nn) != cudaSuccess || s->tris.reserve(nt) != cudaSuccess ||
+      s->spheres.reserve(std::max<uint32_t>(1, nsph)) != cudaSuccess || s->status.reserve(1) != cudaSuccess)
+    return fail(CKR_ERR_OUT_OF_MEMORY);
+  if (!bvh.nodes.empty() &&
+      cudaMemcpy(s->nodes.ptr, bvh.nodes.data(), bvh.nodes.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(CKR_ERR_CUDA);
+  if (!bvh.tris.empty() &&
+      cudaMemcpy(s->tris.ptr, bvh.tris.data(), bvh.tris.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(CKR_ERR_CUDA);
+  if (nsph) {
+    s->host_spheres.assign(sph4, sph4 + 4 * (size_t)nsph);
+    if (cudaMemcpy(s->spheres.ptr, sph4, 4 * sizeof(float) * nsph, cudaMemcpyHostToDevice) != cudaSuccess)
+      return fail(CKR_ERR_CUDA);
+  }
+  if (cudaMemset(s->status.ptr, 0, sizeof(int)) != cudaSuccess) return fail(CKR_ERR_CUDA);
+  s->host_nodes.swap(bvh.nodes);
+  s->host_tris.swap(bvh.tris);
+  *out = s;
+  return CKR_OK;
+}
+
+extern "C" int ckr_scene_destroy(ckr_scene *scene) {
+  if (!scene) return CKR_ERR_INVALID_ARGUMENT;
+  for (auto &st : scene->pipe)
+    if (st) cudaStreamDestroy(st);
+  for (auto &e : scene->ev)
+    if (e) cudaEventDestroy(e);
+  delete scene;
+  return CKR_OK;
+}
+
+extern "C" int ckr_scene_get_info(const ckr_scene *s, ckr_scene_info *out) {
+  if (!s || !out) return CKR_ERR_INVALID_ARGUMENT;
+  std::memset(out, 0, sizeof(*out));
+  out->ntri = s->ntri;
+  out->nsph = s->nsph;
+  out->nnodes = s->nnodes;
+  out->nleaves = s->nleaves;
+  out->max_depth = s->max_depth;
+  out->device_bytes = s->nodes.bytes() + s->tris.bytes() + s->spheres.bytes();
+  out->build_ms = s->build_ms;
+  return CKR_OK;
+}
+
+extern "C" int ckr_scene_check(ckr_scene *s, void *stream) {
+  if (!s) return CKR_ERR_INVALID_ARGUMENT;
+  int h = 0;
+  CKR_CUDA_TRY(cudaMemcpyAsync(&h, s->status.ptr, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  CKR_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  if (h != 0) CKR_CUDA_TRY(cudaMemset(s->status.ptr, 0, sizeof(int)));
+  return h;
+}
+
+extern "C" int ckr_trace_closest(const ckr_scene *s, const ckr_ray *rays, uint32_t n, uint32_t *hit_id,
+                                 float *hit_t, void *stream) {
+  if (!s || (n && (!rays || !hit_id || !hit_t)) || !aligned16(rays)) return CKR_ERR_INVALID_ARGUMENT;
+  return launch_trace<false>(s, rays, n, hit_id, hit_t, nullptr, (cudaStream_t)stream);
+}
+
+extern "C" int ckr_trace_any(const ckr_scene *s, const ckr_ray *rays, uint32_t n, uint8_t *occluded,
+                             void *stream) {
+  if (!s || (n && (!rays || !occluded)) || !aligned16(rays)) return CKR_ERR_INVALID_ARGUMENT;
+  return launch_trace<true>(s, rays, n, nullptr, nullptr, occluded, (cudaStream_t)stream);
+}
+
+namespace {
+
+// Host-buffer path: two internal streams alternate over chunks so that the
+// copy of chunk k+1 overlaps the traversal of chunk k.
+template <bool ANY>
+int trace_host(ckr_scene *s, const ckr_ray *rays, uint32_t n, uint32_t *hit_id, float *hit_t, uint8_t *occ,
+               cudaStream_t user) {
+  if (n == 0) return CKR_OK;
+  std::lock_guard<std::mutex> lock(s->host_mu);
+  const uint32_t chunk = 1u << 20;
+  uint32_t cap = std::min(n, 2 * chunk);
+  CKR_CUDA_TRY(s->st_rays.reserve(cap));
+  if (ANY) {
+    CKR_CUDA_TRY(s->st_occ.reserve(cap));
+  } else {
+    CKR_CUDA_TRY(s->st_id.reserve(cap));
+    CKR_CUDA_TRY(s->st_t.reserve(cap));
+  }
+  for (int k = 0; k < 2; ++k)
+    if (!s->pipe[k]) CKR_CUDA_TRY(cudaStreamCreateWithFlags(&s->pipe[k], cudaStreamNonBlocking));
+  for (int k = 0; k < 4; ++k)
+    if (!s->ev[k]) CKR_CUDA_TRY(cudaEventCreateWithFlags(&s->ev[k], cudaEventDisableTiming));
+  // Order after prior work on the caller's stream.
+  CKR_CUDA_TRY(cudaEventRecord(s->ev[2], user));
+  CKR_CUDA_TRY(cudaStreamWaitEvent(s->pipe[0], s->ev[2], 0));
+  CKR_CUDA_TRY(cudaStreamWaitEvent(s->pipe[1], s->ev[2], 0));
+  uint32_t k = 0;
+  for (uint32_t off = 0; off < n; off += chunk, ++k) {
+    uint32_t m = std::min(chunk, n - off);
+    int slot = k & 1;
+    cudaStream_t st = s->pipe[slot];
+    size_t base = (size_t)slot * chunk;
+    CKR_CUDA_TRY(cudaMemcpyAsync(s->st_rays.ptr + base, rays + off, (size_t)m * sizeof(ckr_ray),
+                                 cudaMemcpyHostToDevice, st));
+    int rc = ANY ? launch_trace<true>(s, s->st_rays.ptr + base, m, nullptr, nullptr, s->st_occ.ptr + base, st)
+                 : launch_trace<false>(s, s->st_rays.ptr + base, m, s->st_id.ptr + base, s->st_t.ptr + base,
+                                       nullptr, st);
+    if (rc != CKR_OK) return rc;
+    if (ANY) {
+      CKR_CUDA_TRY(cudaMemcpyAsync(occ + off, s->st_occ.ptr + base, m, cudaMemcpyDeviceToHost, st));
+    } else {
+      CKR_CUDA_TRY(cudaMemcpyAsync(hit_id + off, s->st_id.ptr + base, (size_t)m * 4, cudaMemcpyDeviceToHost, st));
+      CKR_CUDA_TRY(cudaMemcpyAsync(hit_t + off, s->st_t.ptr + base, (size_t)m * 4, cudaMemcpyDeviceToHost, st));
+    }
+  }
+  CKR_CUDA_TRY(cudaEventRecord(s->ev[0], s->pipe[0]));
+  CKR_CUDA_TRY(cudaEventRecord(s->ev[1], s->pipe[1]));
+  CKR_CUDA_TRY(cudaStreamWaitEvent(user, s->ev[0], 0));
+  CKR_CUDA_TRY(cudaStreamWaitEvent(user, s->ev[1], 0));
+  CKR_CUDA_TRY(cudaStreamSynchronize(user));
+  int h = 0;
+  CKR_CUDA_TRY(cudaMemcpy(&h, s->status.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h != 0) {
+    CKR_CUDA_TRY(cudaMemset(s->status.ptr, 0, sizeof(int)));
+    return h;
+  }
+  return CKR_OK;
+}
+
+}  // namespace
+
+extern "C" int ckr_trace_closest_host(ckr_scene *s, const ckr_ray *rays, uint32_t n, uint32_t *hit_id,
+                                      float *hit_t, void *stream) {
+  if (!s || (n && (!rays || !hit_id || !hit_t))) return CKR_ERR_INVALID_ARGUMENT;
+  return trace_host<false>(s, rays, n, hit_id, hit_t, nullptr, (cudaStream_t)stream);
+}
+
+extern "C" int ckr_trace_any_host(ckr_scene *s, const ckr_ray *rays, uint32_t n, uint8_t *occluded,
+                                  void *stream) {
+  if (!s || (n && (!rays || !occluded))) return CKR_ERR_INVALID_ARGUMENT;
+  return trace_host<true>(s, rays, n, nullptr, nullptr, occluded, (cudaStream_t)stream);
+}
+
+namespace ckr {
+// Accessors for the host statistics replay (trace_stats.cpp).
+void scene_host_arrays(const ckr_scene *s, const float **nodes, const float **tris, const float **spheres,
+                       int32_t *root, uint32_t *nsph, uint32_t *depth) {
+  *nodes = s->host_nodes.data();
+  *tris = s->host_tris.data();
+  *spheres = s->host_spheres.data();
+  *root = s->root;
+  *nsph = s->nsph;
+  *depth = s->max_depth;
+}
+}  // namespace ckr

@@ -1,0 +1,185 @@
+// workloads.cpp — deterministic synthetic inputs (icosphere mesh, ray sets).
+//
+// No reference counterpart: the reference renders hand-written XML scenes.
+// These generators stand in for the benchmark scenes.  They use only
+// +, -, *, /, sqrt and floor in FP64 (compiled with -ffp-contract=off), so
+// x86-64 and aarch64 produce bit-identical outputs.
+#include <cmath>
+#include <cstring>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/ckr.h"
+#include "ckr_rng.h"
+
+namespace {
+
+struct D3 {
+  double x, y, z;
+};
+
+inline D3 d3(double x, double y, double z) { return D3{x, y, z}; }
+inline D3 add(D3 a, D3 b) { return d3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline D3 sub(D3 a, D3 b) { return d3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline D3 mul(D3 a, double s) { return d3(a.x * s, a.y * s, a.z * s); }
+inline double dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline D3 cross(D3 a, D3 b) { return d3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+inline D3 normalize(D3 a) { return mul(a, 1.0 / std::sqrt(dot(a, a))); }
+
+// Lattice value in [-1, 1) for integer point (ix, iy, iz).
+inline double lattice(uint64_t seed, int64_t ix, int64_t iy, int64_t iz) {
+  uint64_t h = ckr_mix64(seed ^ ((uint64_t)ix * 0x8CB92BA72F3D8DD7ull));
+  h = ckr_mix64(h ^ ((uint64_t)iy * 0xD6E8FEB86659FD93ull));
+  h = ckr_mix64(h ^ ((uint64_t)iz * 0xA0761D6478BD642Full));
+  return (double)(h >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}
+
+// Quintic fade 6t^5 - 15t^4 + 10t^3.
+inline double fade(double t) { return t * t * t * (t * (t * 6.0 - 15.0) + 10.0); }
+
+double value_noise(uint64_t seed, double x, double y, double z) {
+  double fx = std::floor(x), fy = std::floor(y), fz = std::floor(z);
+  int64_t ix = (int64_t)fx, iy = (int64_t)fy, iz = (int64_t)fz;
+  double u = fade(x - fx), v = fade(y - fy), w = fade(z - fz);
+  double c[2][2][2];
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b)
+      for (int d = 0; d < 2; ++d) c[a][b][d] = lattice(seed, ix + a, iy + b, iz + d);
+  double x00 = c[0][0][0] + (c[1][0][0] - c[0][0][0]) * u;
+  double x10 = c[0][1][0] + (c[1][1][0] - c[0][1][0]) * u;
+  double x01 = c[0][0][1] + (c[1][0][1] - c[0][0][1]) * u;
+  double x11 = c[0][1][1] + (c[1][1][1] - c[0][1][1]) * u;
+  double y0 = x00 + (x10 - x00) * v;
+  double y1 = x01 + (x11 - x01) * v;
+  return y0 + (y1 - y0) * w;
+}
+
+double fbm(uint64_t seed, D3 p, uint32_t octaves) {
+  double sum = 0.0, norm = 0.0, amp = 1.0, freq = 2.0;
+  for (uint32_t o = 0; o < octaves; ++o) {
+    uint64_t s = ckr_mix64(seed + 0x9E3779B97F4A7C15ull * (o + 1));
+    sum += amp * value_noise(s, p.x * freq, p.y * freq, p.z * freq);
+    norm += amp;
+    amp *= 0.5;
+    freq *= 2.0;
+  }
+  return norm > 0.0 ? sum / norm : 0.0;
+}
+
+}  // namespace
+
+extern "C" int ckr_workload_icosphere(uint32_t subdiv, float noise_amp, uint32_t octaves,
+                                      uint64_t seed, float *tri9_out, uint32_t capacity,
+                                      uint32_t *ntri_out) {
+  if (subdiv > 10 || !ntri_out) return CKR_ERR_INVALID_ARGUMENT;
+  uint64_t ntri = 20ull << (2 * subdiv);
+  *ntri_out = (uint32_t)ntri;
+  if (!tri9_out) return CKR_OK;  // size query
+  if (capacity < ntri) return CKR_ERR_TOO_LARGE;
+
+  const double phi = (1.0 + std::sqrt(5.0)) * 0.5;
+  std::vector<D3> v = {d3(-1, phi, 0), d3(1, phi, 0),  d3(-1, -phi, 0), d3(1, -phi, 0),
+                       d3(0, -1, phi), d3(0, 1, phi),  d3(0, -1, -phi), d3(0, 1, -phi),
+                       d3(phi, 0, -1), d3(phi, 0, 1),  d3(-phi, 0, -1), d3(-phi, 0, 1)};
+  for (auto &p : v) p = normalize(p);
+  std::vector<uint32_t> f = {0, 11, 5, 0, 5,  1, 0, 1, 7, 0, 7,  10, 0, 10, 11, 1, 5, 9, 5, 11,
+                             4, 11, 10, 2, 10, 7, 6, 7, 1, 8,  3, 9,  4,  3, 4, 2, 3, 2, 6, 3,
+                             6, 8, 3, 8,  9, 4, 9, 5, 2, 4,  11, 6, 2,  10, 8, 6, 7, 9, 8, 1};
+  for (uint32_t level = 0; level < subdiv; ++level) {
+    std::unordered_map<uint64_t, uint32_t> mid;
+    mid.reserve(f.size());
+    auto midpoint = [&](uint32_t a, uint32_t b) -> uint32_t {
+      uint64_t key = a < b ? ((uint64_t)a << 32 | b) : ((uint64_t)b << 32 | a);
+      auto it = mid.find(key);
+      if (it != mid.end()) return it->second;
+      v.push_back(normalize(mul(add(v[a], v[b]), 0.5)));
+      uint32_t id = (uint32_t)v.size() - 1;
+      mid.emplace(key, id);
+      return id;
+    };
+    std::vector<uint32_t> g;
+    g.reserve(f.size() * 4);
+    for (size_t i = 0; i < f.size(); i += 3) {
+      uint32_t a = f[i], b = f[i + 1], c = f[i + 2];
+      uint32_t ab = midpoint(a, b), bc = midpoint(b, c), ca = midpoint(c, a);
+      uint32_t quad[12] = {a, ab, ca, b, bc, ab, c, ca, bc, ab, bc, ca};
+      g.insert(g.end(), quad, quad + 12);
+    }
+    f.swap(g);
+  }
+  std::vector<float> pos(v.size() * 3);
+  for (size_t i = 0; i < v.size(); ++i) {
+    double r = 1.0 + (double)noise_amp * fbm(seed, v[i], octaves);
+    pos[3 * i + 0] = (float)(v[i].x * r);
+    pos[3 * i + 1] = (float)(v[i].y * r);
+    pos[3 * i + 2] = (float)(v[i].z * r);
+  }
+  for (size_t t = 0; t < ntri; ++t)
+    for (int k = 0; k < 3; ++k) std::memcpy(tri9_out + 9 * t + 3 * k, &pos[3 * f[3 * t + k]], 3 * sizeof(float));
+  return CKR_OK;
+}
+
+extern "C" int ckr_workload_rays_pinhole(const float eye[3], const float target[3], const float up[3],
+                                         float vfov_deg, uint32_t width, uint32_t height, float tmax,
+                                         ckr_ray *out) {
+  if (!eye || !target || !up || !out || width == 0 || height == 0 || !(vfov_deg > 0.f && vfov_deg < 180.f))
+    return CKR_ERR_INVALID_ARGUMENT;
+  D3 e = d3(eye[0], eye[1], eye[2]);
+  D3 fwd = normalize(sub(d3(target[0], target[1], target[2]), e));
+  D3 right = cross(fwd, d3(up[0], up[1], up[2]));
+  if (dot(right, right) < 1e-30) return CKR_ERR_INVALID_ARGUMENT;
+  right = normalize(right);
+  D3 upv = cross(right, fwd);
+  double th = std::tan((double)vfov_deg * (3.14159265358979323846 / 360.0));
+  double tw = th * (double)width / (double)height;
+  for (uint32_t y = 0; y < height; ++y) {
+    double sy = (1.0 - 2.0 * ((double)y + 0.5) / (double)height) * th;
+    for (uint32_t x = 0; x < width; ++x) {
+      double sx = (2.0 * ((double)x + 0.5) / (double)width - 1.0) * tw;
+      D3 d = normalize(add(add(fwd, mul(right, sx)), mul(upv, sy)));
+      ckr_ray &r = out[(size_t)y * width + x];
+      r.ox = eye[0];
+      r.oy = eye[1];
+      r.oz = eye[2];
+      r.tmin = 0.f;
+      r.dx = (float)d.x;
+      r.dy = (float)d.y;
+      r.dz = (float)d.z;
+      r.tmax = tmax;
+    }
+  }
+  return CKR_OK;
+}
+
+extern "C" int ckr_workload_rays_incoherent(const float lo[3], const float hi[3], uint64_t seed,
+                                            uint32_t n, float tmax_lo, float tmax_hi, ckr_ray *out) {
+  if (!lo || !hi || (!out && n)) return CKR_ERR_INVALID_ARGUMENT;
+  for (uint32_t i = 0; i < n; ++i) {
+    uint64_t key = ckr_key(seed, i);
+    ckr_ray &r = out[i];
+    r.ox = (float)((double)lo[0] + ((double)hi[0] - lo[0]) * ckr_draw_f(key, 0));
+    r.oy = (float)((double)lo[1] + ((double)hi[1] - lo[1]) * ckr_draw_f(key, 1));
+    r.oz = (float)((double)lo[2] + ((double)hi[2] - lo[2]) * ckr_draw_f(key, 2));
+    r.tmin = 0.f;
+    // Marsaglia (1972): (x1, x2) uniform in the unit disc maps to the sphere.
+    double x1, x2, s;
+    uint32_t c = 3;
+    do {
+      x1 = 2.0 * ckr_draw_f(key, c) - 1.0;
+      x2 = 2.0 * ckr_draw_f(key, c + 1) - 1.0;
+      s = x1 * x1 + x2 * x2;
+      c += 2;
+    } while (s >= 1.0 || s == 0.0);
+    double q = 2.0 * std::sqrt(1.0 - s);
+    D3 d = normalize(d3(x1 * q, x2 * q, 1.0 - 2.0 * s));
+    r.dx = (float)d.x;
+    r.dy = (float)d.y;
+    r.dz = (float)d.z;
+    r.tmax = (float)((double)tmax_lo + ((double)tmax_hi - tmax_lo) * ckr_draw_f(key, 1000));
+  }
+  return CKR_OK;
+}
+
+extern "C" float ckr_rng_uniform(uint64_t seed, uint64_t index, uint32_t counter) {
+  return ckr_draw_f(ckr_key(seed, index), counter);
+}

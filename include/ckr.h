@@ -1,0 +1,155 @@
+/*
+ * ckr.h — C ABI of chakumrender_gb300, a GB300 (sm_103a) implementation of the
+ * path-tracing hot path of Sayantan2048/ChakumRender.
+ *
+ * Conventions (every entry point):
+ *   - returns int status: CKR_OK (0) or a negative CKR_ERR_* code; no C++
+ *     exception crosses this boundary; ckr_status_string() names a code;
+ *   - plain pointers and sizes; "device" pointers are CUDA device memory on
+ *     the current device, "host" pointers are ordinary (ideally pinned) memory;
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream);
+ *     entry points that take device buffers are asynchronous on that stream,
+ *     entry points suffixed _host are synchronous and copy inside;
+ *   - scene handles are library-owned device state: create once, query from any
+ *     number of host threads, destroy once.
+ *
+ * Each declaration names the reference interface it replaces (file:line in
+ * the reference repository).
+ */
+#ifndef CKR_H
+#define CKR_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define CKR_OK 0
+#define CKR_ERR_INVALID_ARGUMENT -1
+#define CKR_ERR_CUDA -2
+#define CKR_ERR_OUT_OF_MEMORY -3
+#define CKR_ERR_STACK_OVERFLOW -4 /* traversal stack deeper than the BVH allows */
+#define CKR_ERR_QUEUE_OVERFLOW -5 /* wavefront queue capacity exceeded */
+#define CKR_ERR_ITERATION_LIMIT -6 /* a bounded device loop gave up */
+#define CKR_ERR_NO_DEVICE -7
+#define CKR_ERR_PARSE -8
+#define CKR_ERR_IO -9
+#define CKR_ERR_TOO_LARGE -10
+
+/* Writes a NUL-terminated description of `status` into buf[0..len). */
+int ckr_status_string(int status, char *buf, size_t len);
+
+/* ---- rays and hits ----------------------------------------------------- */
+/* One ray: 32 bytes, two 16-byte loads on the device.  The reference's Ray
+ * (headers/mathPrimitives.h:39-44) is origin + direction in FP64 with no
+ * range; here a ray carries its own (tmin, tmax) interval. */
+typedef struct ckr_ray {
+  float ox, oy, oz, tmin;
+  float dx, dy, dz, tmax;
+} ckr_ray;
+
+/* Hit ids: CKR_MISS on a miss (the reference's id = 0xFFFFFFFF,
+ * src/bvhAccel.cpp:213), the input index of a triangle, or CKR_SPHERE_BIT |
+ * the input index of a sphere.  Ids are in INPUT order; the reference returns
+ * BVH order and reorders its primitive list (src/bvhAccel.cpp:95-124). */
+#define CKR_MISS 0xFFFFFFFFu
+#define CKR_SPHERE_BIT 0x80000000u
+
+/* ---- scene: geometry + BVH in device memory ---------------------------- */
+typedef struct ckr_scene ckr_scene;
+
+typedef struct ckr_build_params {
+  uint32_t max_leaf_size; /* triangles per leaf, 1..8; 0 = default (4) */
+  uint32_t sah_bins;      /* binned-SAH bins, 4..64; 0 = default (16) */
+  uint32_t threads;       /* host build threads; 0 = all cores */
+} ckr_build_params;
+
+typedef struct ckr_scene_info {
+  uint32_t ntri, nsph;
+  uint32_t nnodes;     /* interior nodes (each holds two child boxes) */
+  uint32_t nleaves;
+  uint32_t max_depth;  /* = traversal stack entries needed */
+  uint32_t reserved;
+  uint64_t device_bytes;
+  double build_ms;
+} ckr_scene_info;
+
+/* Replaces loadAccels() (headers/objects.h:17, src/objects.cpp:38-56), which
+ * builds the two BVHs (BvhAccel::initAccel, src/bvhAccel.cpp:13-22) over the
+ * global triangle and sphere lists.  tri9: ntri x (A.xyz, B.xyz, C.xyz);
+ * sph4: nsph x (centre.xyz, radius).  Builds a binned-SAH BVH on the host and
+ * uploads it.  Either list may be empty (NULL, 0). */
+int ckr_scene_create(const float *tri9, uint32_t ntri, const float *sph4, uint32_t nsph,
+                     const ckr_build_params *params, ckr_scene **out);
+int ckr_scene_destroy(ckr_scene *scene);
+int ckr_scene_get_info(const ckr_scene *scene, ckr_scene_info *out);
+
+/* Device status word of the scene: the first error a traversal kernel hit
+ * (CKR_ERR_STACK_OVERFLOW); synchronises `stream`, returns and clears it. */
+int ckr_scene_check(ckr_scene *scene, void *stream);
+
+/* Closest hit.  Replaces BvhAccel::intersectT / intersectS
+ * (headers/bvhAccel.h:73-74, src/bvhAccel.cpp:151-248) and the
+ * intersectTriangle / intersectSphere pair of src/shader.cpp:16-73, which
+ * shade() combines as "sphere if tS < tT".  Device buffers: rays[n] in,
+ * hit_id[n] and hit_t[n] out (hit_t = tmax on a miss).  A triangle is hit
+ * when tmin < t < best-so-far, both faces, edges inclusive, with the
+ * reference's near-parallel rejection (d.n)^2 <= 1e-10 (n the unit normal);
+ * the test itself is watertight (Woop, Benthin, Wald 2013).  A
+ * sphere is hit at the nearest root above max(tmin, 1e-4)
+ * (src/geometryPrimitives.cpp:12-27). */
+int ckr_trace_closest(const ckr_scene *scene, const ckr_ray *rays, uint32_t n,
+                      uint32_t *hit_id, float *hit_t, void *stream);
+
+/* Any hit.  Replaces shadow(ray, dist) (headers/shader.h:6,
+ * src/shader.cpp:76-97): occluded[i] = 1 iff some primitive is hit with
+ * tmin < t < tmax; the caller folds the reference's 1e-5 slack into tmax
+ * (tmax = dist - 1e-5).  Stops at the first hit. */
+int ckr_trace_any(const ckr_scene *scene, const ckr_ray *rays, uint32_t n,
+                  uint8_t *occluded, void *stream);
+
+/* Host-buffer forms of the two queries (the drop-in for callers that hold
+ * rays in host memory, as every reference caller does): copy rays in, trace,
+ * copy results out, in chunks that overlap copies with traversal.  Staging
+ * buffers are owned by the scene and reused. */
+int ckr_trace_closest_host(ckr_scene *scene, const ckr_ray *rays, uint32_t n,
+                           uint32_t *hit_id, float *hit_t, void *stream);
+int ckr_trace_any_host(ckr_scene *scene, const ckr_ray *rays, uint32_t n,
+                       uint8_t *occluded, void *stream);
+
+/* Host replay of the device traversal in the same FP32 arithmetic: mean child
+ * boxes tested and triangles tested per ray (closest-hit mode), used for the
+ * algorithmic-bytes roofline.  rays are host memory. */
+int ckr_trace_stats(const ckr_scene *scene, const ckr_ray *rays, uint32_t n,
+                    double *mean_boxes, double *mean_tris);
+
+/* ---- synthetic workloads (deterministic; no reference counterpart) ----- */
+/* Icosphere: the 20-face icosahedron, `subdiv` midpoint subdivisions
+ * (20 * 4^subdiv triangles), vertices pushed to radius
+ * 1 + noise_amp * fbm(p), fbm = `octaves` octaves of seeded 3-D value noise
+ * (base frequency 2, lacunarity 2, gain 0.5) normalised to [-1, 1]. */
+int ckr_workload_icosphere(uint32_t subdiv, float noise_amp, uint32_t octaves,
+                           uint64_t seed, float *tri9_out, uint32_t capacity,
+                           uint32_t *ntri_out);
+
+/* Pinhole camera rays through pixel centres, row-major from the top-left
+ * pixel, vertical field of view vfov_deg, square pixels; tmin 0. */
+int ckr_workload_rays_pinhole(const float eye[3], const float target[3], const float up[3],
+                              float vfov_deg, uint32_t width, uint32_t height, float tmax,
+                              ckr_ray *out);
+
+/* Incoherent rays: origins uniform in the box [lo, hi], directions uniform on
+ * the unit sphere (Marsaglia 1972), tmax uniform in [tmax_lo, tmax_hi];
+ * ray i is a function of (seed, i) only. */
+int ckr_workload_rays_incoherent(const float lo[3], const float hi[3], uint64_t seed,
+                                 uint32_t n, float tmax_lo, float tmax_hi, ckr_ray *out);
+
+/* The library's counter-based stream (see csrc/ckr_rng.h), for checkers. */
+float ckr_rng_uniform(uint64_t seed, uint64_t index, uint32_t counter);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

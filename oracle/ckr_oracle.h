@@ -1,0 +1,76 @@
+/*
+ * ckr_oracle.h — CPU oracle for the ChakumRender path-tracing hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the shipped library links, loads or
+ * calls this code: it is the checker that the parity tests, the smoke check
+ * and the CPU-baseline leg of bench.py compare the CUDA path against.
+ *
+ * Everything here is a plain-C FP64 restatement of the reference renderer
+ * (Sayantan2048/ChakumRender, C++98, FP64).  Each function names the
+ * reference file:line it follows.  The restatement is pinned against the
+ * reference itself: oracle/Makefile compiles the reference's own sources
+ * into oracle/_ref/libckr_ref.so and tests/test_oracle_pin.py checks that
+ * both give identical answers (bit-identical hit ids and t for traversal).
+ *
+ * Build with -ffp-contract=off so that x86-64 and aarch64 round identically.
+ */
+#ifndef CKR_ORACLE_H
+#define CKR_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_INF 1e20 /* headers/mathPrimitives.h:5 */
+#define ORC_MISS 0xFFFFFFFFu
+
+/* ---------------------------------------------------------------------- */
+/* Traversal: midpoint BVH over FP64 triangles (src/bvhAccel.cpp).        */
+/* ---------------------------------------------------------------------- */
+typedef struct orc_bvh orc_bvh;
+
+/* Build the reference's BVH (centroid-midpoint split, one primitive per leaf,
+ * src/bvhAccel.cpp:13-149) over ntri triangles given as 9 floats each
+ * (A.xyz, B.xyz, C.xyz).  Returns NULL on allocation failure. */
+orc_bvh *orc_bvh_build(const float *tri9, uint32_t ntri);
+void orc_bvh_free(orc_bvh *b);
+uint32_t orc_bvh_node_count(const orc_bvh *b);
+
+/* Rays are 8 floats: ox oy oz tmin dx dy dz tmax (tmin/tmax are ignored by the
+ * closest-hit query, which, like BvhAccel::intersectT, has no t range).
+ * hit_id receives the ORIGINAL triangle index (ORC_MISS on a miss) and hit_t
+ * the FP64 distance (ORC_INF on a miss).  nodes/tris, when non-NULL, receive
+ * per-ray counts of node visits and triangle tests.  threads<=0: all cores. */
+void orc_trace_closest(const orc_bvh *b, const float *rays8, uint32_t nrays,
+                       uint32_t *hit_id, double *hit_t,
+                       uint32_t *nodes, uint32_t *tris, int threads);
+
+/* shadow() semantics (src/shader.cpp:76-97) for a triangle-only scene:
+ * occluded[i] = 1 iff the closest triangle hit t satisfies t + 1e-5 < dist,
+ * with dist = tmax + 1e-5 so that "occluded" means a hit with t < tmax. */
+void orc_trace_shadow(const orc_bvh *b, const float *rays8, uint32_t nrays,
+                      uint8_t *occluded, int threads);
+
+/* Triangle::intersect (src/geometryPrimitives.cpp:29-71) on one triangle, plus
+ * the barycentric margin min(beta, gamma, 1-beta-gamma) (negative: outside)
+ * and |d.n| (the reference rejects rays with (d.n)^2 <= 1e-10). */
+double orc_tri_intersect(const float *tri9, const float *ray8, double *margin,
+                         double *ddotn);
+
+/* Sphere::intersect (src/geometryPrimitives.cpp:12-27). */
+double orc_sphere_intersect(const double *c3, double r, const double *o3,
+                            const double *d3);
+
+/* Signed distance from the ray's plane hit point to the triangle boundary
+ * (negative inside); t_plane receives the plane distance. */
+double orc_tri_edge_distance(const float *tri9, const float *ray8, double *t_plane);
+
+/* Nearest sphere per ray (sph4: centre.xyz, radius); ORC_MISS / ORC_INF on a miss. */
+void orc_spheres_closest(const float *sph4, uint32_t nsph, const float *rays8, uint32_t nrays,
+                         uint32_t *hit_id, double *hit_t);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,129 @@
+"""Generates the golden fixtures in tests/golden/ by running the REFERENCE renderer.
+
+Needs oracle/_ref/libckr_ref.so (built by `make -C oracle ref` from the reference's own
+sources) and libckr.so (for the deterministic input generators).  Run from the repo root:
+
+    python tests/golden/make_golden.py
+
+Fixtures:
+  trace_small.npz        1280-triangle displaced icosphere; pinhole + incoherent rays;
+                         the reference's BvhAccel::intersectT ids/t and shadow() booleans.
+  trace_edges.npz        hand-built adversarial cases (shared edges, vertices, axis-aligned
+                         and zero-component directions, grazing and in-plane rays, origins
+                         on surfaces, degenerate triangles) with the reference's answers.
+  trace_full_sample.npz  the 1,310,720-triangle mesh (digest only) and 4096 sampled rays of
+                         the benchmark ray set with the reference's answers.
+"""
+from __future__ import annotations
+
+import hashlib
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+from chakumrender_gb300 import ckr  # noqa: E402
+import oracle as O  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def ray(o, d, tmax=1e30, tmin=0.0):
+    return np.array([o[0], o[1], o[2], tmin, d[0], d[1], d[2], tmax], dtype=np.float32)
+
+
+def normalize(v):
+    v = np.asarray(v, dtype=np.float64)
+    return (v / np.linalg.norm(v)).astype(np.float32)
+
+
+def edge_cases():
+    rng = np.random.default_rng(11)
+    ico = ckr.icosphere(2, 0.05, 6, 5)  # 320 triangles, shared edges/vertices
+    ground = np.array([[-3, -1.5, -3, 3, -1.5, -3, 3, -1.5, 3],
+                       [-3, -1.5, -3, 3, -1.5, 3, -3, -1.5, 3]], dtype=np.float32)
+    degenerate = np.array([[1e6, 1e6, 1e6, 1e6, 1e6, 1e6, 1e6, 1e6, 1e6]], dtype=np.float32)
+    sliver = np.array([[-2, 2, 0, 2, 2, 0, 0, 2.0001, 0]], dtype=np.float32)
+    wall = np.array([[2.5, -2, -2, 2.5, 2, -2, 2.5, 2, 2]], dtype=np.float32)
+    tri = np.concatenate([ico, ground, degenerate, sliver, wall])
+    rays = []
+    eye = np.array([0.3, 0.2, 4.0], dtype=np.float32)
+    # Rays aimed at edge midpoints and vertices of the icosphere (shared features).
+    for t in ico[rng.choice(len(ico), 64, replace=False)]:
+        a, b, c = t[:3], t[3:6], t[6:]
+        for p in (a, b, c, 0.5 * (a + b), 0.5 * (b + c), 0.5 * (c + a), (a + b + c) / 3):
+            rays.append(ray(eye, normalize(p - eye)))
+    # Axis-aligned directions from several origins (zero direction components).
+    for o in ([0, 0, 3], [0.1, 0.2, -3], [3, 0.05, 0.02], [0, -3, 0.0], [0.2, 0.3, 0.4], [0, 0, 0]):
+        for d in ([0, 0, -1], [0, 0, 1], [1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0]):
+            rays.append(ray(np.float32(o), np.float32(d)))
+    # Rays in the ground plane and parallel to it (near-parallel rejection).
+    for x in np.linspace(-2, 2, 9):
+        rays.append(ray([x, -1.5, -4], [0, 0, 1]))
+        rays.append(ray([x, -1.5 + 1e-4, -4], normalize([0, -1e-6, 1])))
+        rays.append(ray([x, -1.0, -4], normalize([0, -1e-5, 1])))
+        rays.append(ray([x, -1.0, -4], normalize([0, -0.2, 1])))
+    # Grazing rays along the wall, rays hitting the sliver, rays toward the degenerate triangle.
+    for y in np.linspace(-1.9, 1.9, 7):
+        rays.append(ray([2.5, y, -3], [0, 0, 1]))
+        rays.append(ray([0, 2.00005, -3], normalize([0.001 * y, 0, 1])))
+        rays.append(ray([1e6 - 1, 1e6 - 1, 1e6 - 1], normalize([1, 1, 1])))
+    # Origins on the surface (points inside triangles), shooting out and in.
+    for t in ico[rng.choice(len(ico), 32, replace=False)]:
+        a, b, c = t[:3].astype(np.float64), t[3:6].astype(np.float64), t[6:].astype(np.float64)
+        p = ((a + b + c) / 3).astype(np.float32)
+        n = normalize(np.cross(c - a, b - a))
+        rays.append(ray(p, n))
+        rays.append(ray(p, -n))
+        rays.append(ray(p, normalize(rng.normal(size=3))))
+    # Random rays through the whole setup, with shadow distances.
+    for _ in range(256):
+        o = rng.uniform(-3, 3, size=3).astype(np.float32)
+        rays.append(ray(o, normalize(rng.normal(size=3)), tmax=float(rng.uniform(0.01, 5))))
+    return tri, np.stack(rays)
+
+
+def run_reference(tri, rays):
+    rb = O.ReferenceBvh(tri)
+    ids, t = rb.closest(rays)
+    occ = rb.shadow(rays)
+    return ids, t, occ
+
+
+def main():
+    if not O.ref_available():
+        sys.exit("oracle/_ref/libckr_ref.so is missing: run `make -C oracle ref` first")
+    # Small mesh.
+    tri = ckr.icosphere(3, 0.05, 6, 1)
+    lo, hi = tri.reshape(-1, 3).min(0), tri.reshape(-1, 3).max(0)
+    r1 = ckr.rays_pinhole([0, 0, 3], [0, 0, 0], [0, 1, 0], 40.0, 48, 48)
+    r2 = ckr.rays_incoherent(lo, hi, 7, 2048, 0.05, 2.0)
+    rays = np.concatenate([r1, r2])
+    ids, t, occ = run_reference(tri, rays)
+    np.savez_compressed(OUT / "trace_small.npz", tri=tri, rays=rays, ids=ids, t=t, occluded=occ)
+    print("trace_small:", len(tri), "tris", len(rays), "rays", "hit rate", float((ids != 0xFFFFFFFF).mean()))
+
+    tri, rays = edge_cases()
+    ids, t, occ = run_reference(tri, rays)
+    np.savez_compressed(OUT / "trace_edges.npz", tri=tri, rays=rays, ids=ids, t=t, occluded=occ)
+    print("trace_edges:", len(tri), "tris", len(rays), "rays", "hit rate", float((ids != 0xFFFFFFFF).mean()))
+
+    tri = ckr.icosphere(8, 0.05, 6, 1)
+    digest = hashlib.sha256(tri.tobytes()).hexdigest()
+    lo, hi = tri.reshape(-1, 3).min(0), tri.reshape(-1, 3).max(0)
+    r1 = ckr.rays_pinhole([0, 0, 3], [0, 0, 0], [0, 1, 0], 40.0, 2048, 2048)
+    r2 = ckr.rays_incoherent(lo, hi, 7, 4194304, 0.05, 2.0)
+    pick = np.random.default_rng(3).choice(len(r1), 2048, replace=False)
+    rays = np.concatenate([r1[pick], r2[pick]])
+    ids, t, occ = run_reference(tri, rays)
+    np.savez_compressed(OUT / "trace_full_sample.npz", mesh_sha256=np.array(digest), ray_index=pick,
+                        rays=rays, ids=ids, t=t, occluded=occ)
+    print("trace_full_sample:", digest[:16], len(rays), "rays")
+
+
+if __name__ == "__main__":
+    main()

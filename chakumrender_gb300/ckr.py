@@ -71,8 +71,31 @@ def lib() -> C.CDLL:
     _sig(L, "ckr_workload_rays_pinhole", [P, P, P, F32, U32, U32, F32, P])
     _sig(L, "ckr_workload_rays_incoherent", [P, P, C.c_uint64, U32, F32, F32, P])
     _sig(L, "ckr_rng_uniform", [C.c_uint64, C.c_uint64, U32], F32)
+    _sig(L, "ckr_ltc_init", [C.c_char_p])
+    _sig(L, "ckr_ltc_shade", [P, U32, P, P, U32, P, P])
+    _sig(L, "ckr_workload_gbuffer", [C.c_uint64, U32, P])
+    _sig(L, "ckr_workload_quad_lights", [C.c_uint64, U32, F32, F32, F32, P, P])
     _lib = L
     return L
+
+
+def gbuffer(seed: int, npx: int) -> np.ndarray:
+    out = np.empty((npx, 12), dtype=np.float32)
+    check(lib().ckr_workload_gbuffer(seed, npx, _ptr(out)), "gbuffer")
+    return out
+
+
+def quad_lights(seed: int, nquads: int = 8, side_lo: float = 0.2, side_hi: float = 1.0, radiance: float = 5.0):
+    tri = np.empty((2 * nquads, 9), dtype=np.float32)
+    rgb = np.empty((2 * nquads, 3), dtype=np.float32)
+    check(lib().ckr_workload_quad_lights(seed, nquads, side_lo, side_hi, radiance, _ptr(tri), _ptr(rgb)),
+          "quad_lights")
+    return tri, rgb
+
+
+def ltc_shade(gbuf_dev: int, npx: int, light_tri_dev: int, light_rgb_dev: int, nlight: int, rgb_dev: int,
+              stream: int = 0) -> None:
+    check(lib().ckr_ltc_shade(gbuf_dev, npx, light_tri_dev, light_rgb_dev, nlight, rgb_dev, stream), "ckr_ltc_shade")
 
 
 def status_string(status: int) -> str:

@@ -183,3 +183,77 @@ extern "C" int ckr_workload_rays_incoherent(const float lo[3], const float hi[3]
 extern "C" float ckr_rng_uniform(uint64_t seed, uint64_t index, uint32_t counter) {
   return ckr_draw_f(ckr_key(seed, index), counter);
 }
+
+namespace {
+// Orthonormal basis about a unit vector (Duff et al. 2017, "Building an
+// Orthonormal Basis, Revisited").
+void onb(D3 n, D3 &t, D3 &b) {
+  double s = n.z >= 0.0 ? 1.0 : -1.0;
+  double a = -1.0 / (s + n.z);
+  double c = n.x * n.y * a;
+  t = d3(1.0 + s * n.x * n.x * a, s * c, -s * n.x);
+  b = d3(c, s + n.y * n.y * a, -n.y);
+}
+
+// Uniform on the unit sphere from the stream (Marsaglia 1972), from counter c.
+D3 sphere_dir(uint64_t key, uint32_t &c) {
+  double x1, x2, s;
+  do {
+    x1 = 2.0 * ckr_draw_f(key, c) - 1.0;
+    x2 = 2.0 * ckr_draw_f(key, c + 1) - 1.0;
+    s = x1 * x1 + x2 * x2;
+    c += 2;
+  } while (s >= 1.0 || s == 0.0);
+  double q = 2.0 * std::sqrt(1.0 - s);
+  return normalize(d3(x1 * q, x2 * q, 1.0 - 2.0 * s));
+}
+}  // namespace
+
+extern "C" int ckr_workload_gbuffer(uint64_t seed, uint32_t npx, float *out12) {
+  if (!out12 && npx) return CKR_ERR_INVALID_ARGUMENT;
+  for (uint32_t i = 0; i < npx; ++i) {
+    uint64_t key = ckr_key(seed, i);
+    float *g = out12 + 12 * (size_t)i;
+    for (int k = 0; k < 3; ++k) g[k] = (float)(2.0 * ckr_draw_f(key, k) - 1.0);
+    uint32_t c = 16;
+    D3 n = sphere_dir(key, c);
+    if (n.z < 0) n.z = -n.z;  // uniform on the +z hemisphere
+    // View direction: cosine lobe about n (Malley's method on a disc sample).
+    double x1, x2, s;
+    uint32_t c2 = 200;
+    do {
+      x1 = 2.0 * ckr_draw_f(key, c2) - 1.0;
+      x2 = 2.0 * ckr_draw_f(key, c2 + 1) - 1.0;
+      s = x1 * x1 + x2 * x2;
+      c2 += 2;
+    } while (s >= 1.0);
+    D3 t, b;
+    onb(n, t, b);
+    D3 v = normalize(add(add(mul(t, x1), mul(b, x2)), mul(n, std::sqrt(1.0 - s))));
+    g[3] = (float)(0.05 + 0.95 * ckr_draw_f(key, 3));   // GGX alpha in [0.05, 1]
+    g[4] = (float)n.x; g[5] = (float)n.y; g[6] = (float)n.z;
+    g[7] = (float)(0.02 + 0.88 * ckr_draw_f(key, 4));   // F0 in [0.02, 0.9]
+    g[8] = (float)v.x; g[9] = (float)v.y; g[10] = (float)v.z;
+    g[11] = ckr_draw_f(key, 5);                          // specular coefficient in [0, 1)
+  }
+  return CKR_OK;
+}
+
+extern "C" int ckr_workload_quad_lights(uint64_t seed, uint32_t nquads, float side_lo, float side_hi, float radiance,
+                                        float *tri9_out, float *rgb_out) {
+  if ((!tri9_out || !rgb_out) && nquads) return CKR_ERR_INVALID_ARGUMENT;
+  for (uint32_t q = 0; q < nquads; ++q) {
+    uint64_t key = ckr_key(seed, q);
+    double side = side_lo + ((double)side_hi - side_lo) * ckr_draw_f(key, 0);
+    double cx = -2.0 + 4.0 * ckr_draw_f(key, 1), cy = -2.0 + 4.0 * ckr_draw_f(key, 2), cz = 1.0 + 2.0 * ckr_draw_f(key, 3);
+    double h = 0.5 * side;
+    double p[4][3] = {{cx - h, cy - h, cz}, {cx + h, cy - h, cz}, {cx + h, cy + h, cz}, {cx - h, cy + h, cz}};
+    const int tri[2][3] = {{0, 2, 1}, {0, 3, 2}};  // facing -z
+    for (int k = 0; k < 2; ++k)
+      for (int v = 0; v < 3; ++v)
+        for (int j = 0; j < 3; ++j) tri9_out[9 * (2 * q + k) + 3 * v + j] = (float)p[tri[k][v]][j];
+    for (int k = 0; k < 2; ++k)
+      for (int j = 0; j < 3; ++j) rgb_out[3 * (2 * q + k) + j] = radiance;
+  }
+  return CKR_OK;
+}

@@ -125,7 +125,40 @@ int ckr_trace_any_host(ckr_scene *scene, const ckr_ray *rays, uint32_t n,
 int ckr_trace_stats(const ckr_scene *scene, const ckr_ray *rays, uint32_t n,
                     double *mean_boxes, double *mean_tris);
 
+/* ---- LTC polygon-light shading ------------------------------------------ */
+/* Loads the GGX LTC fit table (the reference's headers/ltc.inc, converted to
+ * data/ltc_ggx.bin).  NULL: the copy beside libckr.so.  Optional: the first
+ * shading call loads the default; call before it to use another file. */
+int ckr_ltc_init(const char *table_path);
+
+/* LTC shading of a G-buffer.  Replaces, per pixel,
+ * LightSource::getLightFromMeshSource_Analytic (src/lightSources_CV.cpp:323-333)
+ * with its helpers getLightAnalytic / getLightAnalyticDiffuse / clipTriangle /
+ * integrateEdge (:8-321) and M_GGX + getBrdfApproxParam
+ * (headers/ltc.h:18-61, src/materialTypes.cpp:52-74), for a GGX material with
+ * specularCoef `spec`:
+ *   rgb = spec * amplitude * sum_i L_i |I_ltc,i| / 2pi + (1 - spec) * sum_i L_i |I_cos,i| / 2pi
+ * over the emitter triangles i of one mesh light.  Device buffers:
+ * gbuf[npx] = 12 floats per pixel (pos.xyz, alpha, n.xyz, f0, v.xyz, spec),
+ * v the unit direction towards the viewer (-ray.d), 16-byte aligned;
+ * light_tri9[nlight] (A, B, C), light_rgb[nlight] radiance; rgb[npx] out
+ * (3 floats).  f0 is not used by the LTC (the fit has no Fresnel term). */
+int ckr_ltc_shade(const float *gbuf, uint32_t npx, const float *light_tri9, const float *light_rgb,
+                  uint32_t nlight, float *rgb, void *stream);
+
 /* ---- synthetic workloads (deterministic; no reference counterpart) ----- */
+/* G-buffer for LTC shading (12 floats per pixel as ckr_ltc_shade reads them):
+ * pos uniform in [-1,1]^3, n uniform on the +z hemisphere, v cosine-distributed
+ * about n, alpha uniform in [0.05,1], f0 uniform in [0.02,0.9], spec uniform
+ * in [0,1). */
+int ckr_workload_gbuffer(uint64_t seed, uint32_t npx, float *out12);
+
+/* Axis-aligned square emitters facing -z: side uniform in [side_lo, side_hi],
+ * centre uniform in [-2,2]^2 x [1,3]; two triangles per quad (tri9_out gets
+ * 2*nquads rows), each with radiance (r, r, r). */
+int ckr_workload_quad_lights(uint64_t seed, uint32_t nquads, float side_lo, float side_hi, float radiance,
+                             float *tri9_out, float *rgb_out);
+
 /* Icosphere: the 20-face icosahedron, `subdiv` midpoint subdivisions
  * (20 * 4^subdiv triangles), vertices pushed to radius
  * 1 + noise_amp * fbm(p), fbm = `octaves` octaves of seeded 3-D value noise

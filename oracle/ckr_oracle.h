@@ -70,6 +70,35 @@ double orc_tri_edge_distance(const float *tri9, const float *ray8, double *t_pla
 void orc_spheres_closest(const float *sph4, uint32_t nsph, const float *rays8, uint32_t nrays,
                          uint32_t *hit_id, double *hit_t);
 
+/* ---------------------------------------------------------------------- */
+/* Materials, samplers and LTC shading (orc_shading.c).                   */
+/* ---------------------------------------------------------------------- */
+/* MaterialType (headers/materialTypes.h:21-98); brdf uses the reference's
+ * BRDFType numbering: 0 NONE, 1 CLASSIC_PHONG, 2 GGX, 3 BECKMANN, 4 PHONG,
+ * 5 GGXAPPROX.  `spec` is specularCoef. */
+typedef struct orc_material {
+  int32_t brdf;
+  int32_t pad;
+  double alpha, phong_exp, spec, int_ior, ext_ior;
+} orc_material;
+
+/* Loads the LTC fit table (chakumrender_gb300/data/ltc_ggx.bin). 0 on success. */
+int orc_ltc_load(const char *path);
+/* M_GGX (headers/ltc.h:18-61): lerped M (row-major, stale det of the lower
+ * theta entry), lerped Minv, lerped amplitude. */
+void orc_m_ggx(float theta, float alpha, double *M9, double *detM, double *Minv9, double *amplitude);
+/* MaterialType::brdf and ::pdfEval per row (vectors are 3 doubles per row).
+ * use_ltc: evaluate the LTC-approximate branch with getBrdfApproxParam(force). */
+void orc_brdf_batch(const orc_material *m, uint32_t count, const double *n, const double *wo_ref, const double *wo,
+                    const double *wi, int use_ltc, double *brdf_out, double *pdf_out);
+/* getLightFromMeshSource_Analytic for one shading point (x, n, v = -r.d). */
+void orc_ltc_shade(const orc_material *m, const double *x3, const double *n3, const double *v3,
+                   const float *light_tri9, const float *light_rgb, uint32_t nlight, double *rgb);
+void orc_ltc_shade_batch(const orc_material *m, uint32_t count, const double *x, const double *n, const double *v,
+                         const float *light_tri9, const float *light_rgb, uint32_t nlight, double *rgb, int threads);
+/* One direction sample from uniforms (e1, e2); see orc_shading.c for `kind`. */
+void orc_sample_dir(int kind, const double *n3, const double *w3, double param, double e1, double e2, double *out3);
+
 #ifdef __cplusplus
 }
 #endif

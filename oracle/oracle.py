@@ -15,6 +15,12 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ORACLE_SO = HERE / "liboracle.so"
 REF_SO = HERE / "_ref" / "libckr_ref.so"
+LTC_TABLE = HERE.parent / "chakumrender_gb300" / "data" / "ltc_ggx.bin"
+
+# orc_material / the reference's MaterialType fields (brdf: 0 NONE, 1 CLASSIC_PHONG,
+# 2 GGX, 3 BECKMANN, 4 PHONG, 5 GGXAPPROX).
+MATERIAL = np.dtype([("brdf", "<i4"), ("pad", "<i4"), ("alpha", "<f8"), ("phong_exp", "<f8"), ("spec", "<f8"),
+                     ("int_ior", "<f8"), ("ext_ior", "<f8")])
 
 P = C.c_void_p
 U32 = C.c_uint32
@@ -40,6 +46,13 @@ def orc() -> C.CDLL:
         _sig(L, "orc_tri_intersect", [P, P, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_double)
         _sig(L, "orc_spheres_closest", [P, U32, P, U32, P, P], None)
         _sig(L, "orc_tri_edge_distance", [P, P, C.POINTER(C.c_double)], C.c_double)
+        _sig(L, "orc_ltc_load", [C.c_char_p])
+        _sig(L, "orc_m_ggx", [C.c_float, C.c_float, P, P, P, P], None)
+        _sig(L, "orc_brdf_batch", [P, U32, P, P, P, P, C.c_int, P, P], None)
+        _sig(L, "orc_ltc_shade_batch", [P, U32, P, P, P, P, P, U32, P, C.c_int], None)
+        _sig(L, "orc_sample_dir", [C.c_int, P, P, C.c_double, C.c_double, C.c_double, P], None)
+        if L.orc_ltc_load(str(LTC_TABLE).encode()) != 0:
+            raise RuntimeError(f"cannot load {LTC_TABLE}")
         _orc = L
     return _orc
 
@@ -152,3 +165,59 @@ class ReferenceBvh:
         occ = np.empty(len(rays), dtype=np.uint8)
         ref().ref_trace_shadow(_p(rays), len(rays), _p(occ), threads)
         return occ
+
+
+# ---- materials, samplers, LTC -----------------------------------------------------------
+def _d3(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64).reshape(-1, 3)
+
+
+def m_ggx(theta: float, alpha: float, reference: bool = False):
+    """M_GGX: (M row-major 9, det(M) of the lower theta entry, Minv 9, amplitude)."""
+    M, Mi = np.empty(9), np.empty(9)
+    det, amp = C.c_double(), C.c_double()
+    lib = _ref_shading_sigs() if reference else orc()
+    lib.ref_m_ggx(theta, alpha, _p(M), C.byref(det), _p(Mi), C.byref(amp)) if reference else \
+        lib.orc_m_ggx(theta, alpha, _p(M), C.byref(det), _p(Mi), C.byref(amp))
+    return M, det.value, Mi, amp.value
+
+
+def brdf_batch(mat, n, wo_ref, wo, wi, use_ltc=False, reference=False):
+    """MaterialType::brdf and ::pdfEval per row."""
+    mat = np.ascontiguousarray(mat, dtype=MATERIAL)
+    n, wo_ref, wo, wi = _d3(n), _d3(wo_ref), _d3(wo), _d3(wi)
+    out, pdf = np.empty(len(mat)), np.empty(len(mat))
+    f = _ref_shading_sigs().ref_brdf_batch if reference else orc().orc_brdf_batch
+    f(_p(mat), len(mat), _p(n), _p(wo_ref), _p(wo), _p(wi), int(use_ltc), _p(out), _p(pdf))
+    return out, pdf
+
+
+def ltc_shade_batch(mat, x, n, v, light_tri9, light_rgb, reference=False, threads=0):
+    """getLightFromMeshSource_Analytic per shading point (v = view direction = -r.d)."""
+    mat = np.ascontiguousarray(mat, dtype=MATERIAL)
+    x, n, v = _d3(x), _d3(n), _d3(v)
+    lt = np.ascontiguousarray(light_tri9, dtype=np.float32).reshape(-1, 9)
+    lc = np.ascontiguousarray(light_rgb, dtype=np.float32).reshape(-1, 3)
+    out = np.empty((len(mat), 3))
+    f = _ref_shading_sigs().ref_ltc_shade_batch if reference else orc().orc_ltc_shade_batch
+    f(_p(mat), len(mat), _p(x), _p(n), _p(v), _p(lt), _p(lc), len(lt), _p(out), threads)
+    return out
+
+
+def sample_dir(kind: int, n, w, param: float, e1: float, e2: float) -> np.ndarray:
+    """One direction sample of the reference samplers from uniforms (see orc_shading.c)."""
+    n = np.ascontiguousarray(n, dtype=np.float64).reshape(3)
+    w = np.ascontiguousarray(w if w is not None else n, dtype=np.float64).reshape(3)
+    out = np.empty(3)
+    orc().orc_sample_dir(kind, _p(n), _p(w), param, e1, e2, _p(out))
+    return out
+
+
+def _ref_shading_sigs():
+    L = ref()
+    if not hasattr(L, "_shading"):
+        _sig(L, "ref_m_ggx", [C.c_float, C.c_float, P, P, P, P], None)
+        _sig(L, "ref_brdf_batch", [P, U32, P, P, P, P, C.c_int, P, P], None)
+        _sig(L, "ref_ltc_shade_batch", [P, U32, P, P, P, P, P, U32, P, C.c_int], None)
+        L._shading = True
+    return L

@@ -18,6 +18,7 @@
 #include "objects.h"
 #include "bvhAccel.h"
 #include "shader.h"
+#include "lightSources.h"
 
 extern "C" {
 
@@ -68,6 +69,82 @@ void ref_trace_shadow(const float *rays8, uint32_t nrays, uint8_t *occluded, int
     const float *r = rays8 + 8 * i;
     Ray ray(Vec(r[0], r[1], r[2]), Vec(r[4], r[5], r[6]));
     occluded[i] = shadow(ray, (double)r[7] + 1e-5) < 0.5 ? 1 : 0;
+  }
+}
+
+// ---- materials and LTC shading ------------------------------------------
+// Row layout shared with orc_material (oracle/ckr_oracle.h).
+struct RefMaterialRow {
+  int32_t brdf;
+  int32_t pad;
+  double alpha, phong_exp, spec, int_ior, ext_ior;
+};
+
+static MaterialType make_material(const RefMaterialRow &r) {
+  if (r.brdf == CLASSIC_PHONG) return MaterialType(r.phong_exp, r.spec);
+  return MaterialType(r.alpha, r.int_ior, r.ext_ior, r.spec, (BRDFType)r.brdf);
+}
+
+// MaterialType::brdf (optionally with getBrdfApproxParam(force) first) and pdfEval.
+void ref_brdf_batch(const RefMaterialRow *m, uint32_t count, const double *n, const double *wo_ref,
+                    const double *wo, const double *wi, int use_ltc, double *brdf_out, double *pdf_out) {
+  for (uint32_t i = 0; i < count; ++i) {
+    MaterialType mt = make_material(m[i]);
+    Vec N(n[3 * i], n[3 * i + 1], n[3 * i + 2]), R(wo_ref[3 * i], wo_ref[3 * i + 1], wo_ref[3 * i + 2]);
+    Vec O(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]), I(wi[3 * i], wi[3 * i + 1], wi[3 * i + 2]);
+    BRDFApprox ap;
+    if (use_ltc) mt.getBrdfApproxParam(N, O, ap, true);
+    brdf_out[i] = mt.brdf(N, R, O, I, ap);
+    if (pdf_out) pdf_out[i] = mt.pdfEval(N, R, O, I);
+  }
+}
+
+}  // extern "C"
+
+// Defined in the reference's materialTypes.cpp (via headers/ltc.h); not declared in any header.
+void M_GGX(const float theta, const float alpha, mat3 &M, mat3 &Minv, double &amplitude);
+
+extern "C" {
+
+void ref_m_ggx(float theta, float alpha, double *M9, double *detM, double *Minv9, double *amplitude) {
+  mat3 M, Mi;
+  M_GGX(theta, alpha, M, Mi, *amplitude);
+  for (int k = 0; k < 9; ++k) {
+    M9[k] = M.a[k];
+    Minv9[k] = Mi.a[k];
+  }
+  *detM = M.det;
+}
+
+// LightSource::getLightFromMeshSource_Analytic for each shading point, with one
+// mesh light made of the given emitter triangles (radiance light_rgb per triangle).
+void ref_ltc_shade_batch(const RefMaterialRow *m, uint32_t count, const double *x, const double *n, const double *v,
+                         const float *light_tri9, const float *light_rgb, uint32_t nlight, double *rgb,
+                         int threads) {
+  LightSource ls;
+  MeshLight mesh;
+  for (uint32_t i = 0; i < nlight; ++i) {
+    const float *t = light_tri9 + 9 * (size_t)i;
+    const float *c = light_rgb + 3 * (size_t)i;
+    double mx = c[0] > c[1] ? c[0] : c[1];
+    mx = mx > c[2] ? mx : c[2];
+    mesh.add(TriLight(Vec(t[0], t[1], t[2]), Vec(t[3], t[4], t[5]), Vec(t[6], t[7], t[8]), Vec(c[0], c[1], c[2]),
+                      mx));
+  }
+  mesh.initMeshLight();
+  ls.addMSource(mesh);
+  if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t i = 0; i < (int64_t)count; ++i) {
+    MaterialType mt = make_material(m[i]);
+    Sphere prim(1.0, Vec(0, 0, 0), Vec(1, 1, 1), 1.0, mt);
+    Vec X(x[3 * i], x[3 * i + 1], x[3 * i + 2]), N(n[3 * i], n[3 * i + 1], n[3 * i + 2]);
+    Vec V(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+    Ray r(X, V * -1.0);
+    Vec out = ls.getLightFromMeshSource_Analytic(r, N, X, &prim);
+    rgb[3 * i] = out.x;
+    rgb[3 * i + 1] = out.y;
+    rgb[3 * i + 2] = out.z;
   }
 }
 

@@ -94,9 +94,62 @@ def run_reference(tri, rays):
     return ids, t, occ
 
 
+def unit(rng, n):
+    v = rng.normal(size=(n, 3))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def shading():
+    """The reference's M_GGX, MaterialType::brdf / pdfEval (plain and LTC-approximate)
+    and getLightFromMeshSource_Analytic on random inputs."""
+    rng = np.random.default_rng(21)
+    out = {}
+    mg = np.stack([rng.uniform(0, 1.58, 256), rng.uniform(0, 1.1, 256)], 1).astype(np.float32)
+    res = [O.m_ggx(float(t), float(a), reference=True) for t, a in mg]
+    out.update(mggx_in=mg, mggx_M=np.stack([r[0] for r in res]), mggx_det=np.array([r[1] for r in res]),
+               mggx_Minv=np.stack([r[2] for r in res]), mggx_amp=np.array([r[3] for r in res]))
+    n = 2048
+    nn = unit(rng, n)
+    wo = unit(rng, n)
+    wo[np.sum(wo * nn, 1) < 0] *= -1
+    wi = unit(rng, n)
+    wi[np.sum(wi * nn, 1) < 0] *= -1
+    wo_ref = 2 * np.sum(nn * wo, 1, keepdims=True) * nn - wo
+    mat = np.zeros(n, dtype=O.MATERIAL)
+    mat["brdf"] = rng.integers(1, 5, n)
+    mat["alpha"] = rng.uniform(0.05, 1, n)
+    mat["alpha"][mat["brdf"] == 4] = rng.uniform(1, 200, int(np.sum(mat["brdf"] == 4)))
+    mat["phong_exp"] = rng.uniform(1, 100, n)
+    mat["spec"] = rng.uniform(0, 1, n)
+    mat["int_ior"] = rng.uniform(1.1, 3, n)
+    mat["ext_ior"] = 1.0
+    b, p = O.brdf_batch(mat, nn, wo_ref, wo, wi, reference=True)
+    mat_ltc = mat.copy()
+    mat_ltc["brdf"] = 2
+    mat_ltc["alpha"] = rng.uniform(0.05, 1, n)
+    bl, _ = O.brdf_batch(mat_ltc, nn, wo_ref, wo, wi, use_ltc=True, reference=True)
+    out.update(brdf_mat=mat, brdf_mat_ltc=mat_ltc, brdf_n=nn, brdf_wo_ref=wo_ref, brdf_wo=wo, brdf_wi=wi,
+               brdf_out=b, brdf_pdf=p, brdf_out_ltc=bl)
+    g = ckr.gbuffer(31, 1024)
+    lt, lc = ckr.quad_lights(32, 8)
+    m = np.zeros(len(g), dtype=O.MATERIAL)
+    m["brdf"] = 2
+    m["alpha"] = g[:, 3]
+    m["spec"] = g[:, 11]
+    f0 = g[:, 7].astype(np.float64)
+    m["int_ior"] = (1 + np.sqrt(f0)) / (1 - np.sqrt(f0))
+    m["ext_ior"] = 1.0
+    x, nrm, v = g[:, 0:3].astype(np.float64), g[:, 4:7].astype(np.float64), g[:, 8:11].astype(np.float64)
+    rgb = O.ltc_shade_batch(m, x, nrm, v, lt, lc, reference=True)
+    out.update(ltc_gbuf=g, ltc_mat=m, ltc_x=x, ltc_n=nrm, ltc_v=v, ltc_tri=lt, ltc_rgb=lc, ltc_out=rgb)
+    return out
+
+
 def main():
     if not O.ref_available():
         sys.exit("oracle/_ref/libckr_ref.so is missing: run `make -C oracle ref` first")
+    np.savez_compressed(OUT / "shading.npz", **shading())
+    print("shading: written")
     # Small mesh.
     tri = ckr.icosphere(3, 0.05, 6, 1)
     lo, hi = tri.reshape(-1, 3).min(0), tri.reshape(-1, 3).max(0)

@@ -1,0 +1,97 @@
+"""CPU checks of the LTC shading path: the FP64 oracle against the reference (golden
+fixture), and the FP32 per-pixel code of ckr_ltc_shade (host replay) against the oracle."""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as O
+from chakumrender_gb300 import ckr
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def materials_from_gbuffer(g):
+    m = np.zeros(len(g), dtype=O.MATERIAL)
+    m["brdf"] = 2  # GGX
+    m["alpha"] = g[:, 3]
+    m["spec"] = g[:, 11]
+    f0 = g[:, 7].astype(np.float64)
+    m["int_ior"] = (1 + np.sqrt(f0)) / (1 - np.sqrt(f0))
+    m["ext_ior"] = 1.0
+    return m
+
+
+def oracle_ltc(g, lt, lc):
+    return O.ltc_shade_batch(materials_from_gbuffer(g), g[:, 0:3], g[:, 4:7], g[:, 8:11], lt, lc)
+
+
+def host_replay(g, lt, lc):
+    f = ckr.lib().ckr_internal_ltc_shade_host
+    f.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
+    f.restype = C.c_int
+    g = np.ascontiguousarray(g, np.float32)
+    out = np.empty((len(g), 3), np.float32)
+    assert f(g.ctypes.data, len(g), lt.ctypes.data, lc.ctypes.data, len(lt), out.ctypes.data) == 0
+    return out
+
+
+def ltc_errors(got, ref):
+    """Per-pixel error relative to the pixel's own magnitude (floored at 1e-3 of the
+    image mean, below which a pixel carries no visible energy)."""
+    mag = np.maximum(np.abs(ref).max(axis=1), 1e-3 * np.abs(ref).mean())
+    return np.abs(got - ref).max(axis=1) / mag
+
+
+def test_oracle_matches_reference_golden():
+    g = np.load(GOLD / "shading.npz")
+    out = O.ltc_shade_batch(g["ltc_mat"], g["ltc_x"], g["ltc_n"], g["ltc_v"], g["ltc_tri"], g["ltc_rgb"])
+    assert np.array_equal(out, g["ltc_out"])
+    for k in range(len(g["mggx_in"])):
+        th, al = g["mggx_in"][k]
+        M, det, Mi, amp = O.m_ggx(float(th), float(al))
+        assert np.array_equal(M, g["mggx_M"][k]) and det == g["mggx_det"][k]
+        assert np.array_equal(Mi, g["mggx_Minv"][k]) and amp == g["mggx_amp"][k]
+    b, p = O.brdf_batch(g["brdf_mat"], g["brdf_n"], g["brdf_wo_ref"], g["brdf_wo"], g["brdf_wi"])
+    assert np.array_equal(b, g["brdf_out"]) and np.array_equal(p, g["brdf_pdf"])
+    b, _ = O.brdf_batch(g["brdf_mat_ltc"], g["brdf_n"], g["brdf_wo_ref"], g["brdf_wo"], g["brdf_wi"], use_ltc=True)
+    assert np.array_equal(b, g["brdf_out_ltc"])
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference sources not built here")
+def test_oracle_matches_live_reference():
+    g = ckr.gbuffer(5, 3000)
+    lt, lc = ckr.quad_lights(6, 8)
+    m = materials_from_gbuffer(g)
+    a = O.ltc_shade_batch(m, g[:, 0:3], g[:, 4:7], g[:, 8:11], lt, lc)
+    b = O.ltc_shade_batch(m, g[:, 0:3], g[:, 4:7], g[:, 8:11], lt, lc, reference=True)
+    assert np.array_equal(a, b)
+
+
+def test_fp32_ltc_replay_vs_oracle():
+    g = ckr.gbuffer(11, 20000)
+    lt, lc = ckr.quad_lights(12, 8)
+    ref = oracle_ltc(g, lt, lc)
+    got = host_replay(g, lt, lc)
+    err = ltc_errors(got, ref)
+    assert err.max() <= 1e-4, np.sort(err)[-10:]
+
+
+def test_gbuffer_distributions():
+    g = ckr.gbuffer(1, 50000)
+    n, v = g[:, 4:7].astype(np.float64), g[:, 8:11].astype(np.float64)
+    assert np.allclose(np.linalg.norm(n, axis=1), 1, atol=1e-6) and np.all(n[:, 2] >= 0)
+    assert np.allclose(np.linalg.norm(v, axis=1), 1, atol=1e-6)
+    c = np.sum(n * v, axis=1)
+    assert np.all(c >= -1e-6)
+    assert abs(np.mean(c) - 2 / 3) < 0.01  # E[cos] under a cosine lobe
+    assert abs(n[:, 2].mean() - 0.5) < 0.01  # uniform hemisphere
+    assert g[:, 3].min() >= 0.05 and g[:, 3].max() <= 1.0
+    assert g[:, 7].min() >= 0.02 and g[:, 7].max() <= 0.9
+    lt, lc = ckr.quad_lights(2, 8)
+    assert lt.shape == (16, 9) and np.all(lc == 5)
+    z = lt.reshape(-1, 3)[:, 2]
+    assert z.min() >= 1 and z.max() <= 3

@@ -185,6 +185,89 @@ def cpu_baseline(tri, closest):
              "incoherent": [float(nv[half:].mean()), float(nt[half:].mean())]})
 
 
+def bench_box_render(torch, steps: int):
+    """Box scene (unit cube, 10 walls, ceiling quad light, GGX + Phong spheres), 256x256,
+    16 spp, max depth 4, MIS light+BRDF, Russian roulette 0.3, seed 1: the wavefront path
+    tracer.  Returns samples/s and Mrays/s (closest-hit + shadow rays)."""
+    from chakumrender_gb300 import scene as S
+
+    sd = S.load_xml(S.SCENES / "box.xml")
+    cam = sd.camera
+    cfg = S.render_cfg(shader=S.SHADER_PATH, spp=16, max_depth=4, n_light=1, n_brdf=1, rr_prob=0.3, seed=1)
+    scene = S.RenderScene(sd)
+    rgb = torch.empty((cam.height, cam.width, 3), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(2):
+        scene.render(cam, cfg, rgb.data_ptr(), None, stream.cuda_stream)
+    torch.cuda.synchronize()
+    scene.ray_stats(reset=True)
+    k = max(3, min(steps, 20))
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(k):
+        scene.render(cam, cfg, rgb.data_ptr(), None, stream.cuda_stream)
+    b.record(stream)
+    torch.cuda.synchronize()
+    sec = a.elapsed_time(b) / 1e3
+    closest, shadow = scene.ray_stats(reset=True)
+    samples = cam.width * cam.height * cfg.spp * k
+    return {"workload": "box scene 256x256, 16 spp, depth 4, MIS (1 light + 1 BRDF sample), RR 0.3",
+            "ms_per_frame": round(1e3 * sec / k, 3), "samples_per_s": round(samples / sec, 1),
+            "mrays_per_s": round((closest + shadow) / sec / 1e6, 2),
+            "rays_per_sample": round((closest + shadow) / samples, 3)}
+
+
+def bench_ltc(torch, steps: int):
+    """LTC shading of a 1024x1024 G-buffer lit by 8 quad lights (16 emitter triangles)."""
+    from chakumrender_gb300 import ckr
+
+    n = 1024 * 1024
+    g = torch.from_numpy(ckr.gbuffer(2, n)).cuda()
+    lt, lc = ckr.quad_lights(3, 8)
+    dt, dc = torch.from_numpy(lt).cuda(), torch.from_numpy(lc).cuda()
+    out = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        ckr.ltc_shade(g.data_ptr(), n, dt.data_ptr(), dc.data_ptr(), len(lt), out.data_ptr(), stream.cuda_stream)
+    k = max(3, min(steps, 50))
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(k):
+        ckr.ltc_shade(g.data_ptr(), n, dt.data_ptr(), dc.data_ptr(), len(lt), out.data_ptr(), stream.cuda_stream)
+    b.record(stream)
+    torch.cuda.synchronize()
+    sec = a.elapsed_time(b) / 1e3 / k
+    return {"workload": "LTC shading, 1024x1024 G-buffer, 8 quad lights", "ms_per_frame": round(1e3 * sec, 4),
+            "mpixels_per_s": round(n / sec / 1e6, 1), "io_gb_per_s": round(n * 60 / sec / 1e9, 1)}
+
+
+def cpu_side_baselines(tri_unused=None):
+    """FP64 restatements of the reference on the host cores for the box render
+    (path tracer, 64x64 x 16 spp sample) and LTC shading (65,536 pixels)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    from chakumrender_gb300 import ckr
+    from chakumrender_gb300 import scene as S
+
+    cores = os.cpu_count() or 1
+    sd = S.load_xml(S.SCENES / "box.xml")
+    cam = sd.camera
+    cam.width = cam.height = 64
+    cfg = S.render_cfg(shader=S.SHADER_PATH, spp=16, max_depth=4, n_light=1, n_brdf=1, rr_prob=0.3, seed=1)
+    t0 = time.perf_counter()
+    O.render(sd, cam, cfg, threads=cores)
+    box = 64 * 64 * 16 / (time.perf_counter() - t0)
+    g = ckr.gbuffer(2, 65536)
+    lt, lc = ckr.quad_lights(3, 8)
+    m = np.zeros(len(g), dtype=O.MATERIAL)
+    m["brdf"], m["alpha"], m["spec"], m["int_ior"], m["ext_ior"] = 2, g[:, 3], g[:, 11], 1.5, 1.0
+    t0 = time.perf_counter()
+    O.ltc_shade_batch(m, g[:, 0:3], g[:, 4:7], g[:, 8:11], lt, lc, threads=cores)
+    ltc = 65536 / (time.perf_counter() - t0)
+    return {"box_samples_per_s": round(box, 1), "ltc_mpixels_per_s": round(ltc / 1e6, 4), "cores": cores,
+            "kind": "port"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -318,10 +401,13 @@ def main():
         "kernel_ms_min_max": [round(min(kernel_ms), 4), round(max(kernel_ms), 4)],
         "clocks": clocks,
     }
+    line["box_render"] = bench_box_render(torch, args.steps)
+    line["ltc_shade"] = bench_ltc(torch, args.steps)
     if not args.no_cpu_baseline:
         cb, ref_counts = cpu_baseline(tri, closest)
         line["cpu_baseline"] = cb
         line["roofline"]["reference_bvh_counts"] = ref_counts
+        line["cpu_baseline_other"] = cpu_side_baselines()
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -1,0 +1,77 @@
+// scene.h — the library-owned scene (geometry, BVH, shading data) shared by the
+// traversal and rendering translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <vector>
+
+#include "ckr_internal.h"
+#include "trace_device.cuh"
+
+namespace ckr {
+
+// Device form of one light source (ckr_light + precomputed sampling data).
+struct DevLight {
+  int32_t type;      // CKR_LIGHT_*
+  uint32_t first;    // MESH/TRI: first emitter triangle; SPHERE: sphere index
+  uint32_t count;    // MESH: emitter triangles
+  uint32_t cdf;      // MESH: offset of its 300-entry inverse CDF in the cdf table
+  float area;        // MESH/TRI: total emitter area (the pdf's 1/area)
+  float px, py, pz;  // POINT: position; SPHERE: centre
+  float radius;      // SPHERE
+  float pr, pg, pb;  // POINT: power
+};
+
+constexpr uint32_t kInvCdfBins = 300;  // MeshLight::invCDFBins (headers/lightSources.h:150)
+
+struct ShadeView {
+  const ckr_material *mats;
+  const uint32_t *tri_mat;   // per input triangle
+  const float *tri9;         // input-order vertices (shading normals, light sampling)
+  const uint32_t *sph_mat;
+  const float4 *sph;         // centre, radius
+  const DevLight *lights;     // sorted: sphere, mesh, triangle, point lights
+  uint32_t nlights;
+  uint32_t first_point;      // index of the first point light (= number of area/sphere lights)
+  const uint32_t *cdf;       // mesh-light inverse CDFs (triangle offsets within the light)
+};
+
+}  // namespace ckr
+
+struct ckr_scene {
+  int device = 0;
+  ckr::DevBuf<float4> nodes, tris, spheres;
+  ckr::DevBuf<int> status;
+  int32_t root = ckr::kDone;
+  uint32_t ntri = 0, nsph = 0, nnodes = 0, nleaves = 0, max_depth = 0;
+  double build_ms = 0.0;
+  std::vector<float> host_nodes, host_tris;  // kept for the host statistics replay
+  std::vector<float> host_spheres;
+  // Shading data (ckr_scene_create_ex only).
+  bool has_shading = false;
+  ckr::DevBuf<ckr_material> mats;
+  ckr::DevBuf<uint32_t> tri_mat, sph_mat, cdf;
+  ckr::DevBuf<float> tri9;
+  ckr::DevBuf<ckr::DevLight> lights;
+  uint32_t nlights = 0, first_point = 0;
+  std::vector<ckr_material> host_mats;
+  std::vector<ckr::DevLight> host_lights;
+  // Renderer work buffers (path state, queues), grown on demand, owned here.
+  void *render_ws = nullptr;
+  void (*render_ws_free)(void *) = nullptr;
+  // Staging for the host-buffer entry points.
+  std::mutex host_mu;
+  ckr::DevBuf<ckr_ray> st_rays;
+  ckr::DevBuf<uint32_t> st_id;
+  ckr::DevBuf<float> st_t;
+  ckr::DevBuf<uint8_t> st_occ;
+  cudaStream_t pipe[2] = {nullptr, nullptr};
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+namespace ckr {
+SceneView view_of(const ckr_scene *s);
+uint32_t stack_depth_of(const ckr_scene *s);
+ShadeView shade_view_of(const ckr_scene *s);
+}  // namespace ckr

@@ -1,0 +1,134 @@
+// scene_ex.cpp — ckr_scene_create_ex: geometry + BVH (ckr_scene_create) plus the
+// shading data the renderer needs (materials, per-primitive material ids,
+// input-order triangles, light sources with their sampling tables).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "scene.h"
+
+namespace ckr {
+
+ShadeView shade_view_of(const ckr_scene *s) {
+  ShadeView v;
+  v.mats = s->mats.ptr;
+  v.tri_mat = s->tri_mat.ptr;
+  v.tri9 = s->tri9.ptr;
+  v.sph_mat = s->sph_mat.ptr;
+  v.sph = s->spheres.ptr;
+  v.lights = s->lights.ptr;
+  v.nlights = s->nlights;
+  v.first_point = s->first_point;
+  v.cdf = s->cdf.ptr;
+  return v;
+}
+
+namespace {
+
+// Triangle::area (headers/geometryPrimitives.h:70-76): 0.5 |(C - A) x (B - A)| in FP64.
+double tri_area(const float *t) {
+  double bx = (double)t[3] - t[0], by = (double)t[4] - t[1], bz = (double)t[5] - t[2];
+  double cx = (double)t[6] - t[0], cy = (double)t[7] - t[1], cz = (double)t[8] - t[2];
+  double nx = cy * bz - cz * by, ny = cz * bx - cx * bz, nz = cx * by - cy * bx;
+  return 0.5 * std::sqrt(nx * nx + ny * ny + nz * nz);
+}
+
+// MeshLight::initMeshLight (src/lightSources.cpp:784-807).
+double build_inv_cdf(const float *tri9, uint32_t first, uint32_t count, uint32_t *inv) {
+  double area = 0;
+  for (uint32_t i = 0; i < count; ++i) area += tri_area(tri9 + 9 * (size_t)(first + i));
+  double cdf = 0;
+  uint32_t last = 0;
+  for (uint32_t i = 0; i < count; ++i) {
+    cdf += tri_area(tri9 + 9 * (size_t)(first + i)) / area;
+    uint32_t index = (uint32_t)(cdf * kInvCdfBins);
+    if (index >= kInvCdfBins) index = kInvCdfBins - 1;
+    for (uint32_t j = last; j <= index; ++j) inv[j] = i;
+    last = index + 1;
+  }
+  for (uint32_t i = last; i < kInvCdfBins; ++i) inv[i] = count - 1;
+  return area;
+}
+
+template <typename T>
+int upload(DevBuf<T> &buf, const T *src, size_t n) {
+  if (buf.reserve(n ? n : 1) != cudaSuccess) return CKR_ERR_OUT_OF_MEMORY;
+  if (n && cudaMemcpy(buf.ptr, src, n * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) return CKR_ERR_CUDA;
+  return CKR_OK;
+}
+
+}  // namespace
+}  // namespace ckr
+
+using namespace ckr;
+
+extern "C" int ckr_scene_create_ex(const ckr_scene_desc *d, ckr_scene **out) {
+  if (!d || !out || (d->ntri && !d->tri9) || (d->nsph && !d->sph4) || (d->nlights && !d->lights) ||
+      (d->nmaterials && !d->materials))
+    return CKR_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  uint32_t nm = d->nmaterials;
+  for (uint32_t i = 0; i < d->ntri; ++i)
+    if ((d->tri_material ? d->tri_material[i] : 0) >= std::max<uint32_t>(nm, 1) || (!nm)) return CKR_ERR_INVALID_ARGUMENT;
+  for (uint32_t i = 0; i < d->nsph; ++i)
+    if ((d->sph_material ? d->sph_material[i] : 0) >= std::max<uint32_t>(nm, 1) || (!nm)) return CKR_ERR_INVALID_ARGUMENT;
+  // Light tables.
+  std::vector<DevLight> lights(d->nlights);
+  std::vector<uint32_t> cdf;
+  for (uint32_t k = 0; k < d->nlights; ++k) {
+    const ckr_light &L = d->lights[k];
+    DevLight &g = lights[k];
+    std::memset(&g, 0, sizeof(g));
+    g.type = L.type;
+    g.first = L.first;
+    g.count = L.count;
+    g.px = L.pos[0]; g.py = L.pos[1]; g.pz = L.pos[2];
+    g.pr = L.power[0]; g.pg = L.power[1]; g.pb = L.power[2];
+    if (L.type == CKR_LIGHT_MESH) {
+      if (L.count == 0 || (uint64_t)L.first + L.count > d->ntri) return CKR_ERR_INVALID_ARGUMENT;
+      g.cdf = (uint32_t)cdf.size();
+      cdf.resize(cdf.size() + kInvCdfBins);
+      g.area = (float)build_inv_cdf(d->tri9, L.first, L.count, &cdf[g.cdf]);
+    } else if (L.type == CKR_LIGHT_TRI) {
+      if (L.first >= d->ntri) return CKR_ERR_INVALID_ARGUMENT;
+      g.count = 1;
+      g.area = (float)tri_area(d->tri9 + 9 * (size_t)L.first);
+    } else if (L.type == CKR_LIGHT_SPHERE) {
+      if (L.first >= d->nsph) return CKR_ERR_INVALID_ARGUMENT;
+      const float *s = d->sph4 + 4 * (size_t)L.first;
+      g.px = s[0]; g.py = s[1]; g.pz = s[2];
+      g.radius = s[3];
+    } else if (L.type != CKR_LIGHT_POINT) {
+      return CKR_ERR_INVALID_ARGUMENT;
+    }
+  }
+  // The reference's MIS::getSamples visits sphere, mesh and triangle sources in
+  // that order (src/mis.cpp:100-146); point lights are handled separately.
+  auto rank = [](int32_t t) { return t == CKR_LIGHT_SPHERE ? 0 : t == CKR_LIGHT_MESH ? 1 : t == CKR_LIGHT_TRI ? 2 : 3; };
+  std::stable_sort(lights.begin(), lights.end(),
+                   [&](const DevLight &a, const DevLight &b) { return rank(a.type) < rank(b.type); });
+  uint32_t first_point = 0;
+  while (first_point < lights.size() && lights[first_point].type != CKR_LIGHT_POINT) ++first_point;
+  ckr_scene *s = nullptr;
+  int st = ckr_scene_create(d->tri9, d->ntri, d->sph4, d->nsph, &d->build, &s);
+  if (st != CKR_OK) return st;
+  std::vector<uint32_t> tm(d->ntri, 0), sm(d->nsph, 0);
+  if (d->tri_material) std::memcpy(tm.data(), d->tri_material, 4 * (size_t)d->ntri);
+  if (d->sph_material) std::memcpy(sm.data(), d->sph_material, 4 * (size_t)d->nsph);
+  if ((st = upload(s->mats, d->materials, nm)) != CKR_OK || (st = upload(s->tri_mat, tm.data(), tm.size())) != CKR_OK ||
+      (st = upload(s->sph_mat, sm.data(), sm.size())) != CKR_OK ||
+      (st = upload(s->tri9, d->tri9, 9 * (size_t)d->ntri)) != CKR_OK ||
+      (st = upload(s->lights, lights.data(), lights.size())) != CKR_OK ||
+      (st = upload(s->cdf, cdf.data(), cdf.size())) != CKR_OK) {
+    ckr_scene_destroy(s);
+    return st;
+  }
+  s->nlights = d->nlights;
+  s->first_point = first_point;
+  s->host_mats.assign(d->materials, d->materials + nm);
+  s->host_lights = lights;
+  s->has_shading = true;
+  *out = s;
+  return CKR_OK;
+}

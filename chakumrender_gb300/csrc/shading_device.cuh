@@ -145,13 +145,15 @@ SHD float pdf_eval(const Material &m, F3 n, F3 wo_ref, F3 wo, F3 wi) {
 }
 
 // ---- samplers (src/domainSampler.cpp) ------------------------------------------
-// Tangent frame of the reference (src/domainSampler.cpp:163-176).
+// Tangent frame of the reference (src/domainSampler.cpp:163-176):
+// X = normalize((-n.y - n.z) / n.x, 1, 1) when n.x != 0, else
+// normalize(1, -n.z / n.y, 1), else (1, 1, 0)/sqrt 2.  Evaluated as
+// sign(n.x) normalize(-n.y - n.z, n.x, n.x) (the same vector), which cannot
+// overflow in FP32 when |n.x| is tiny.
 SHD void ref_frame(F3 n, F3 &X, F3 &Y) {
-  F3 nx;
-  if (n.x != 0.f) nx = f3((-n.y - n.z) / n.x, 1.0f, 1.0f);
-  else if (n.y != 0.f) nx = f3(1.0f, -n.z / n.y, 1.0f);
-  else nx = f3(1.0f, 1.0f, 0.0f);
-  X = normalize(nx);
+  if (n.x != 0.f) X = normalize(f3(-n.y - n.z, n.x, n.x)) * (n.x > 0.f ? 1.0f : -1.0f);
+  else if (n.y != 0.f) X = normalize(f3(n.y, -n.z, n.y)) * (n.y > 0.f ? 1.0f : -1.0f);
+  else X = normalize(f3(1.0f, 1.0f, 0.0f));
   Y = normalize(cross(n, X));
 }
 SHD F3 to_world(F3 X, F3 Y, F3 Z, float x, float y, float z) { return X * x + Y * y + Z * z; }
@@ -289,9 +291,18 @@ SHD F3 mul(const M3f &m, F3 v) {
 
 // getBrdfApproxParam (src/materialTypes.cpp:52-74): Minv . R^T with R^T's rows
 // (T1, T2, n), T1 the tangent in the plane of n and wo.
+// At (near) normal incidence wo - n (n.wo) vanishes; the reference then
+// normalises a zero vector (NaN).  The fit is isotropic at theta = 0, so the
+// sampling frame's X axis is used there instead.
 SHD M3f ltc_minv_world(const LtcLookup &L, F3 n, F3 wo) {
-  F3 T1 = normalize(wo - n * dot(n, wo));
-  F3 T2 = normalize(cross(n, T1));
+  F3 t = wo - n * dot(n, wo);
+  F3 T1, T2;
+  if (dot(t, t) < 1e-12f) {
+    ref_frame(n, T1, T2);
+  } else {
+    T1 = normalize(t);
+  }
+  T2 = normalize(cross(n, T1));
   // Minv = [[mi0, 0, mi2], [0, mi4, 0], [mi6, 0, mi8]]
   M3f r;
   r.a[0] = L.mi[0] * T1.x + L.mi[1] * n.x;

@@ -13,26 +13,8 @@
 
 #include "bvh_build.h"
 #include "ckr_internal.h"
+#include "scene.h"
 #include "trace_device.cuh"
-
-struct ckr_scene {
-  int device = 0;
-  ckr::DevBuf<float4> nodes, tris, spheres;
-  ckr::DevBuf<int> status;
-  int32_t root = ckr::kDone;
-  uint32_t ntri = 0, nsph = 0, nnodes = 0, nleaves = 0, max_depth = 0;
-  double build_ms = 0.0;
-  std::vector<float> host_nodes, host_tris;  // kept for the host statistics replay
-  std::vector<float> host_spheres;
-  // Staging for the host-buffer entry points.
-  std::mutex host_mu;
-  ckr::DevBuf<ckr_ray> st_rays;
-  ckr::DevBuf<uint32_t> st_id;
-  ckr::DevBuf<float> st_t;
-  ckr::DevBuf<uint8_t> st_occ;
-  cudaStream_t pipe[2] = {nullptr, nullptr};
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-};
 
 namespace ckr {
 
@@ -171,6 +153,7 @@ extern "C" int ckr_scene_destroy(ckr_scene *scene) {
     if (st) cudaStreamDestroy(st);
   for (auto &e : scene->ev)
     if (e) cudaEventDestroy(e);
+  if (scene->render_ws && scene->render_ws_free) scene->render_ws_free(scene->render_ws);
   delete scene;
   return CKR_OK;
 }

@@ -38,6 +38,7 @@ struct RayPre {
   float mz0, mz1, mz2;
 };
 
+#if defined(__CUDACC__)
 __device__ __forceinline__ RayPre make_ray(float4 a, float4 b) {
   RayPre r;
   r.ox = a.x; r.oy = a.y; r.oz = a.z; r.tmin = a.w;
@@ -203,4 +204,5 @@ __device__ __forceinline__ uint32_t trace_ray(const SceneView &s, const RayPre &
   return best;
 }
 
+#endif  // __CUDACC__
 }  // namespace ckr

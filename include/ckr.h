@@ -125,6 +125,113 @@ int ckr_trace_any_host(ckr_scene *scene, const ckr_ray *rays, uint32_t n,
 int ckr_trace_stats(const ckr_scene *scene, const ckr_ray *rays, uint32_t n,
                     double *mean_boxes, double *mean_tris);
 
+/* ---- full scenes: materials, lights, rendering --------------------------- */
+/* MaterialType + BasePrimitive colour/reflectance (headers/materialTypes.h:21-98,
+ * headers/geometryPrimitives.h:22-34).  brdf uses the reference's BRDFType
+ * numbering (0 NONE, 1 CLASSIC_PHONG, 2 GGX, 3 BECKMANN, 4 PHONG, 5 GGXAPPROX);
+ * light_type its LightType (0 NONE, 1 POINT, 2 VOLUME, 3 PLANAR, 4 MESH); a
+ * primitive whose material has light_type != 0 is an emitter of `radiance`. */
+typedef struct ckr_material {
+  int32_t brdf;
+  int32_t light_type;
+  float alpha;       /* GGX/Beckmann roughness, microfacet-Phong exponent */
+  float phong_exp;   /* CLASSIC_PHONG exponent */
+  float spec;        /* specularCoef in [0, 1] */
+  float int_ior, ext_ior;
+  float reflectance;
+  float color[3];    /* primitive colour c (multiplies shaded light) */
+  float radiance[3]; /* emitters */
+  float pad[2];
+} ckr_material;
+
+#define CKR_LIGHT_MESH 0   /* MeshLight: emitter triangles [first, first+count) */
+#define CKR_LIGHT_TRI 1    /* TriLight: one emitter triangle `first` */
+#define CKR_LIGHT_SPHERE 2 /* SphereSource: emitter sphere `first` */
+#define CKR_LIGHT_POINT 3  /* PointSource at pos with power `power` */
+
+/* One entry of the reference's LightSource lists (headers/lightSources.h:155-249). */
+typedef struct ckr_light {
+  int32_t type;
+  uint32_t first, count;
+  float pos[3];
+  float power[3];
+  float pad;
+} ckr_light;
+
+typedef struct ckr_scene_desc {
+  const float *tri9;            /* ntri x (A, B, C), emitter triangles included */
+  const uint32_t *tri_material; /* ntri material indices (NULL: all 0) */
+  uint32_t ntri;
+  const float *sph4;            /* nsph x (centre, radius) */
+  const uint32_t *sph_material;
+  uint32_t nsph;
+  const ckr_material *materials;
+  uint32_t nmaterials;
+  const ckr_light *lights;
+  uint32_t nlights;
+  ckr_build_params build;
+} ckr_scene_desc;
+
+/* Scene with shading data (prepareObjects + prepareLightSources + loadAccels +
+ * loadLightSampler, src/prepareScene.cpp:54-280, src/mis.cpp:225-233).  Mesh
+ * lights keep the reference's 300-bin area CDF (src/lightSources.cpp:784-807). */
+int ckr_scene_create_ex(const ckr_scene_desc *desc, ckr_scene **out);
+
+/* Camera of src/main.cpp:77 and src/prepareScene.cpp:12-36: the ray through
+ * pixel (x, y) with sub-pixel offset (jx, jy) has direction
+ * normalize(cx ((x + jx)/w - .5) + cy ((y + jy)/h - .5) + dir); y = 0 is the
+ * bottom row; output pixel index (h - 1 - y) w + x (top row first). */
+typedef struct ckr_camera {
+  float pos[3], dir[3], cx[3], cy[3];
+  uint32_t width, height;
+} ckr_camera;
+
+#define CKR_SHADER_DIRECT_MISCV 0 /* shadeDirectOnly + getLightFromMeshSource_Analytic_MISCV (reference default) */
+#define CKR_SHADER_DIRECT_MIS 1   /* shadeDirectOnly + getLightFromAllSources_MIS */
+#define CKR_SHADER_PATH 2         /* path tracer: MIS light/BRDF at every vertex, BRDF-sampled continuation */
+
+typedef struct ckr_render_cfg {
+  uint32_t shader;           /* CKR_SHADER_* */
+  uint32_t spp;              /* samples per pixel; sample k < 8 uses the reference's fixed
+                                sub-pixel offsets (src/main.cpp:23-24), later ones (0, 0) */
+  uint32_t max_depth;        /* path vertices (CKR_SHADER_PATH) */
+  uint32_t n_light_samples;  /* MIS samples per area/sphere light (reference: 10) */
+  uint32_t n_brdf_samples;   /* MIS BRDF samples (reference: 60; the path tracer uses 1) */
+  float rr_prob;             /* Russian-roulette termination probability (reference: 0.3) */
+  uint64_t seed;             /* per-pixel stream key = hash(seed, pixel index) */
+  uint32_t flags;            /* reserved, 0 */
+  uint32_t reserved;
+} ckr_render_cfg;
+
+/* Renders linear RGB (3 floats per pixel, top row first) into rgb (device),
+ * the mean over spp; accum (device, nullable) receives the FP64 per-pixel sums.
+ * Replaces the OpenMP pixel loop of src/main.cpp:62-94 over shade(). */
+int ckr_render(ckr_scene *scene, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb, double *accum,
+               void *stream);
+
+/* Rays traced by ckr_render on this scene since the last reset: closest-hit
+ * rays (camera + continuation) and shadow rays.  Synchronises the device. */
+int ckr_render_stats(ckr_scene *scene, uint64_t *closest_rays, uint64_t *shadow_rays, int reset);
+
+/* Host form: rgb is host memory (w * h * 3 floats). */
+int ckr_render_host(ckr_scene *scene, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb, void *stream);
+
+/* Scene XML (the reference's schema: SCREEN, CAMERA, MESHOBJECT, SPHEREOBJECT,
+ * MESHSOURCE, TRISOURCE, POINTSOURCE, SPHERESOURCE).  Replaces
+ * initSceneParser + prepareScreenCamera + prepareObjects + prepareLightSources
+ * (headers/prepareScene.h:7-10, src/prepareScene.cpp, src/sceneParser.cpp):
+ * objects first (with the reference's dummy sphere and degenerate dummy
+ * triangle), then light sources, whose emitters are also visible primitives.
+ * ckr_xml_get fills a ckr_scene_desc pointing into the loaded scene's arrays
+ * (valid until ckr_xml_free) and the camera. */
+typedef struct ckr_xml_scene ckr_xml_scene;
+int ckr_xml_load(const char *path, ckr_xml_scene **out);
+int ckr_xml_get(const ckr_xml_scene *scene, ckr_scene_desc *desc, ckr_camera *cam);
+int ckr_xml_free(ckr_xml_scene *scene);
+
+/* P3 PPM of src/main.cpp:98-117: clamp to [0, 1], gamma 1/2.2, int(x*255+.5). */
+int ckr_write_ppm(const char *path, const float *rgb, uint32_t width, uint32_t height);
+
 /* ---- LTC polygon-light shading ------------------------------------------ */
 /* Loads the GGX LTC fit table (the reference's headers/ltc.inc, converted to
  * data/ltc_ggx.bin).  NULL: the copy beside libckr.so.  Optional: the first

@@ -46,6 +46,9 @@ void orc_trace_closest(const orc_bvh *b, const float *rays8, uint32_t nrays,
                        uint32_t *hit_id, double *hit_t,
                        uint32_t *nodes, uint32_t *tris, int threads);
 
+/* BvhAccel::intersectT for one FP64 ray: input triangle index or ORC_MISS. */
+uint32_t orc_bvh_closest1(const orc_bvh *b, const double *o3, const double *d3, double *t);
+
 /* shadow() semantics (src/shader.cpp:76-97) for a triangle-only scene:
  * occluded[i] = 1 iff the closest triangle hit t satisfies t + 1e-5 < dist,
  * with dist = tmax + 1e-5 so that "occluded" means a hit with t < tmax. */
@@ -96,6 +99,15 @@ void orc_ltc_shade(const orc_material *m, const double *x3, const double *n3, co
                    const float *light_tri9, const float *light_rgb, uint32_t nlight, double *rgb);
 void orc_ltc_shade_batch(const orc_material *m, uint32_t count, const double *x, const double *n, const double *v,
                          const float *light_tri9, const float *light_rgb, uint32_t nlight, double *rgb, int threads);
+/* Renders with the reference's shaders restated in FP64 (see orc_render.inc):
+ * desc/cam/cfg are the library's ABI structs (include/ckr.h); rgb receives
+ * width*height*3 doubles, top row first, the mean over cfg->spp. */
+struct ckr_scene_desc;
+struct ckr_camera;
+struct ckr_render_cfg;
+void orc_render(const struct ckr_scene_desc *desc, const struct ckr_camera *cam, const struct ckr_render_cfg *cfg,
+                double *rgb, int threads);
+
 /* One direction sample from uniforms (e1, e2); see orc_shading.c for `kind`. */
 void orc_sample_dir(int kind, const double *n3, const double *w3, double param, double e1, double e2, double *out3);
 

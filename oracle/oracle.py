@@ -221,3 +221,16 @@ def _ref_shading_sigs():
         _sig(L, "ref_ltc_shade_batch", [P, U32, P, P, P, P, P, U32, P, C.c_int], None)
         L._shading = True
     return L
+
+
+def render(scene_data, cam, cfg, threads: int = 0) -> np.ndarray:
+    """The reference's shaders restated in FP64 with the library's RNG streams:
+    (height, width, 3) linear RGB, top row first (chakumrender_gb300.scene structs)."""
+    L = orc()
+    if not hasattr(L, "_render"):
+        _sig(L, "orc_render", [P, P, P, P, C.c_int], None)
+        L._render = True
+    d = scene_data.desc()
+    out = np.empty((cam.height, cam.width, 3), np.float64)
+    L.orc_render(C.byref(d), C.byref(cam), C.byref(cfg), _p(out), threads)
+    return out

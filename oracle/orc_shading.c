@@ -277,12 +277,21 @@ static double pdf_eval(const orc_material *m, V3 n, V3 wo_ref, V3 wo, V3 wi) {
   }
   return spec + diffuse;
 }
+static void ref_frame(V3 n, V3 *X, V3 *Y);
+
 /* src/materialTypes.cpp:52-74 */
 static void brdf_approx_param(const orc_material *m, V3 n, V3 wo, int force, Approx *ap) {
   if (m->brdf == B_GGXAPPROX || (m->brdf == B_GGX && force)) {
     m_ggx((float)acos(vdot(n, wo)), (float)m->alpha, &ap->M, &ap->Minv, &ap->amplitude);
     V3 T1 = vsub(wo, vmul(n, vdot(n, wo)));
-    T1 = vnorm(T1);
+    if (vdot(T1, T1) == 0.0) {
+      /* Exact normal incidence: the reference normalises a zero vector (NaN);
+       * the fit is isotropic there, so take the sampling frame's X axis. */
+      V3 Y;
+      ref_frame(n, &T1, &Y);
+    } else {
+      T1 = vnorm(T1);
+    }
     V3 T2 = vnorm(vcross(n, T1));
     M3 rot_inv = m3_transpose(m3_cols(T1, T2, n));
     ap->Minv = m3_mul(ap->Minv, rot_inv);
@@ -540,3 +549,5 @@ void orc_sample_dir(int kind, const double *n3, const double *w3, double param, 
   }
   out3[0] = r.x; out3[1] = r.y; out3[2] = r.z;
 }
+
+#include "orc_render.inc"

@@ -348,6 +348,16 @@ static uint32_t intersect_t(const orc_bvh *b, V3 o, V3 d, double *t_out,
   return id == ORC_MISS ? ORC_MISS : b->order[id];
 }
 
+/* One ray, FP64 origin/direction: BvhAccel::intersectT.  Returns the input
+ * triangle index or ORC_MISS; *t = distance (ORC_INF on a miss). */
+uint32_t orc_bvh_closest1(const orc_bvh *b, const double *o3, const double *d3, double *t) {
+  if (!b) {
+    *t = ORC_INF;
+    return ORC_MISS;
+  }
+  return intersect_t(b, v3(o3[0], o3[1], o3[2]), v3(d3[0], d3[1], d3[2]), t, NULL, NULL);
+}
+
 static int nthreads(int threads) {
 #ifdef _OPENMP
   return threads > 0 ? threads : omp_get_max_threads();

@@ -19,6 +19,7 @@
 #include "bvhAccel.h"
 #include "shader.h"
 #include "lightSources.h"
+#include "prepareScene.h"
 
 extern "C" {
 
@@ -96,6 +97,75 @@ void ref_brdf_batch(const RefMaterialRow *m, uint32_t count, const double *n, co
     if (use_ltc) mt.getBrdfApproxParam(N, O, ap, true);
     brdf_out[i] = mt.brdf(N, R, O, I, ap);
     if (pdf_out) pdf_out[i] = mt.pdfEval(N, R, O, I);
+  }
+}
+
+}  // extern "C"
+
+// ---- scene loading --------------------------------------------------------
+// initSceneParser + prepareScreenCamera + prepareObjects + prepareLightSources,
+// then the resulting global primitive lists.  Call once per process (the
+// reference keeps them in globals and appends).  Per triangle 9 vertex
+// doubles; per sphere centre + radius; per primitive 16 material doubles:
+// brdf, light type, alpha, phongExp, specularCoef, intIOR, extIOR,
+// reflectance, colour(3), radiance(3), pad(2).  cam: pos, dir, cx, cy, w, h.
+extern "C" {
+
+int ref_scene_load(const char *path, double *cam14, uint32_t *ntri, uint32_t *nsph) {
+  if (!initSceneParser(path)) return -1;
+  uint32_t w, h;
+  Vec pos, dir, cx, cy;
+  if (!prepareScreenCamera(w, h, pos, dir, cx, cy, false)) return -2;
+  if (!prepareObjects(false)) return -3;
+  if (!prepareLightSources(false)) return -4;
+  Vec v[4] = {pos, dir, cx, cy};
+  for (int k = 0; k < 4; ++k) {
+    cam14[3 * k] = v[k].x;
+    cam14[3 * k + 1] = v[k].y;
+    cam14[3 * k + 2] = v[k].z;
+  }
+  cam14[12] = w;
+  cam14[13] = h;
+  *ntri = vTriangleList.size();
+  *nsph = vSphereList.size();
+  return 0;
+}
+
+static void dump_material(const BasePrimitive &p, double *m) {
+  // MaterialType::b is private; brdf() of a probe direction is not needed:
+  // the harness reads the type through the class layout's public neighbours.
+  const MaterialType &mt = p.m;
+  m[0] = -1;  // filled by the caller from the layout below
+  m[1] = mt.l;
+  m[2] = mt.alpha;
+  m[3] = mt.phongExp;
+  m[4] = mt.specularCoef;
+  m[5] = mt.intIOR;
+  m[6] = mt.extIOR;
+  m[7] = p.reflectance;
+  m[8] = p.c.x; m[9] = p.c.y; m[10] = p.c.z;
+  m[11] = mt.radiance.x; m[12] = mt.radiance.y; m[13] = mt.radiance.z;
+  m[14] = m[15] = 0;
+}
+
+void ref_scene_dump(double *tri9, double *sph4, double *tri_mat16, double *sph_mat16) {
+  for (size_t i = 0; i < vTriangleList.size(); ++i) {
+    const Triangle &t = vTriangleList[i];
+    Vec v[3] = {t.A, t.B, t.C};
+    for (int k = 0; k < 3; ++k) {
+      tri9[9 * i + 3 * k] = v[k].x;
+      tri9[9 * i + 3 * k + 1] = v[k].y;
+      tri9[9 * i + 3 * k + 2] = v[k].z;
+    }
+    dump_material(t, tri_mat16 + 16 * i);
+  }
+  for (size_t i = 0; i < vSphereList.size(); ++i) {
+    const Sphere &s = vSphereList[i];
+    sph4[4 * i] = s.p.x;
+    sph4[4 * i + 1] = s.p.y;
+    sph4[4 * i + 2] = s.p.z;
+    sph4[4 * i + 3] = s.r;
+    dump_material(s, sph_mat16 + 16 * i);
   }
 }
 

@@ -145,9 +145,50 @@ def shading():
     return out
 
 
+def read_p3(path):
+    t = Path(path).read_text().split()
+    w, h = int(t[1]), int(t[2])
+    return np.array(t[4:4 + w * h * 3], dtype=np.uint8).reshape(h, w, 3)
+
+
+def reference_images():
+    """The reference binary (oracle/_ref/a.out, default shader: shadeDirectOnly +
+    getLightFromMeshSource_Analytic_MISCV, 1 spp at sub-pixel offset (0.34, 0.20))
+    rendering the box scene and the reference's own scene0.xml; 8-bit P3 output."""
+    import shutil
+    import subprocess
+    import tempfile
+
+    exe = ROOT / "oracle" / "_ref" / "a.out"
+    scenes = {"box": ROOT / "chakumrender_gb300" / "scenes" / "box.xml",
+              "scene0": Path("/root/reference/scene0.xml")}
+    out = {}
+    for name, xml in scenes.items():
+        with tempfile.TemporaryDirectory() as d:
+            shutil.copy(xml, Path(d) / "scene.xml")
+            subprocess.run([str(exe), "scene.xml"], cwd=d, check=True, capture_output=True,
+                           env={"OMP_NUM_THREADS": "8", "PATH": "/usr/bin:/bin"})
+            out[name] = read_p3(Path(d) / "image.ppm")
+    return out
+
+
 def main():
     if not O.ref_available():
         sys.exit("oracle/_ref/libckr_ref.so is missing: run `make -C oracle ref` first")
+    np.savez_compressed(OUT / "ref_images.npz", **reference_images())
+    print("reference images: written")
+    # The reference's own scenes as parsed by the library's loader (which the CPU
+    # tests check against the reference's prepareScene), for GPU tests on hosts
+    # without the reference checkout.
+    sys.path.insert(0, str(ROOT / "tests"))
+    from chakumrender_gb300 import scene as S
+    from scene_io import to_arrays
+
+    arrays = {}
+    for name in ("scene0", "scene1"):
+        arrays.update(to_arrays(S.load_xml(f"/root/reference/{name}.xml"), name))
+    np.savez_compressed(OUT / "ref_scenes.npz", **arrays)
+    print("reference scenes: written")
     np.savez_compressed(OUT / "shading.npz", **shading())
     print("shading: written")
     # Small mesh.

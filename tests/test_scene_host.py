@@ -1,0 +1,124 @@
+"""CPU checks of the scene API and the FP64 render oracle:
+- the XML loader (ckr_xml_load) against the reference's own prepareScene output;
+- the oracle's reference-default shader (shadeDirectOnly + MISCV, 1 spp) against the
+  reference binary's images (golden fixture), statistically (different RNG streams);
+- PPM writer and argument handling."""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as O
+from chakumrender_gb300 import scene as S
+from scene_io import block_agreement, from_arrays, same_scene, srgb8
+
+GOLD = Path(__file__).resolve().parent / "golden"
+REF = Path("/root/reference")
+BOX = S.SCENES / "box.xml"
+
+
+@pytest.mark.skipif(not (O.ref_available() and REF.exists()), reason="reference not available here")
+@pytest.mark.parametrize("name", ["scene0", "scene1", "box"])
+def test_loader_matches_reference_prepare_scene(name, tmp_path):
+    import subprocess
+    import sys
+
+    path = str(BOX if name == "box" else REF / f"{name}.xml")
+    # The reference keeps its scene in process globals: query it in a child process.
+    code = f"""
+import sys, ctypes as C, numpy as np
+sys.path[:0] = {[str(Path(O.__file__).parent)]}
+import oracle as O
+L = O.ref()
+L.ref_scene_load.argtypes = [C.c_char_p, C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+L.ref_scene_dump.argtypes = [C.c_void_p] * 4
+cam = np.zeros(14); nt = C.c_uint32(); ns = C.c_uint32()
+assert L.ref_scene_load({path!r}.encode(), cam.ctypes.data, C.byref(nt), C.byref(ns)) == 0
+tri = np.zeros((nt.value, 9)); sph = np.zeros((ns.value, 4))
+tm = np.zeros((nt.value, 16)); sm = np.zeros((ns.value, 16))
+L.ref_scene_dump(tri.ctypes.data, sph.ctypes.data, tm.ctypes.data, sm.ctypes.data)
+np.savez({str(tmp_path / 'ref.npz')!r}, cam=cam, tri=tri, sph=sph, tm=tm, sm=sm)
+"""
+    subprocess.run([sys.executable, "-c", code], check=True, capture_output=True)
+    r = np.load(tmp_path / "ref.npz")
+    sd = S.load_xml(path)
+    assert np.array_equal(r["tri"].astype(np.float32), sd.tri9)
+    assert np.array_equal(r["sph"].astype(np.float32), sd.sph4)
+    c = sd.camera
+    ours = np.array(list(c.pos) + list(c.dir) + list(c.cx) + list(c.cy) + [c.width, c.height], np.float32)
+    assert np.array_equal(ours, r["cam"].astype(np.float32))
+
+    def row(m):
+        return [m.light_type, m.alpha, m.phong_exp, m.spec, m.int_ior, m.ext_ior, m.reflectance, *m.color, *m.radiance]
+
+    for ids, ref in ((sd.tri_mat, r["tm"]), (sd.sph_mat, r["sm"])):
+        ours = np.array([row(sd.materials[i]) for i in ids], np.float32).reshape(-1, 13)
+        assert np.array_equal(ours, ref[:, 1:14].astype(np.float32))
+
+
+@pytest.mark.skipif(not REF.exists(), reason="reference scenes not available here")
+def test_loader_matches_committed_fixture():
+    g = np.load(GOLD / "ref_scenes.npz")
+    for name in ("scene0", "scene1"):
+        assert same_scene(S.load_xml(REF / f"{name}.xml"), from_arrays(g, name))
+
+
+def image_stats(ours8, ref8):
+    d = np.abs(ours8.astype(np.int64) - ref8.astype(np.int64))
+    return float(d.mean()), float(np.quantile(d, 0.99)), float((d > 8).mean())
+
+
+@pytest.mark.parametrize("name", ["box", "scene0"])
+def test_oracle_default_shader_matches_reference_image(name):
+    """Same scene, camera and sub-pixel offset; the MIS residual is noisy, the LTC
+    term deterministic, so the 8-bit images agree up to that noise."""
+    ref8 = np.load(GOLD / "ref_images.npz")[name]
+    sd = S.load_xml(BOX) if name == "box" else from_arrays(np.load(GOLD / "ref_scenes.npz"), "scene0")
+    img = O.render(sd, sd.camera, S.render_cfg(shader=S.SHADER_DIRECT_MISCV, spp=1, n_light=10, n_brdf=60))
+    mean, p99 = block_agreement(img, ref8)
+    assert mean <= 0.01 and p99 <= 0.1, (mean, p99)
+    if name == "box":  # low-noise scene: also per pixel
+        mean, p99, frac8 = image_stats(srgb8(img), ref8)
+        assert mean < 1.0 and p99 <= 8 and frac8 < 0.02, (mean, p99, frac8)
+
+
+def test_oracle_shaders_are_consistent():
+    """Box scene: MIS and MISCV direct lighting estimate the same integral (MISCV ignores
+    shadows in the reference, so only unshadowed regions are compared); the path tracer
+    adds indirect light."""
+    sd = S.load_xml(BOX)
+    cam = sd.camera
+    cam.width = cam.height = 64
+    mis = O.render(sd, cam, S.render_cfg(shader=S.SHADER_DIRECT_MIS, spp=64, n_light=10, n_brdf=60))
+    path = O.render(sd, cam, S.render_cfg(shader=S.SHADER_PATH, spp=64, max_depth=4))
+    assert np.all(np.isfinite(mis)) and np.all(np.isfinite(path))
+    assert path.mean() > mis.mean() * 1.1  # indirect light adds energy
+    d1 = O.render(sd, cam, S.render_cfg(shader=S.SHADER_PATH, spp=64, max_depth=1))
+    # Depth 1 path tracing is direct lighting by MIS (one light + one BRDF sample).
+    assert abs(d1.mean() - mis.mean()) / mis.mean() < 0.03
+
+
+def test_ppm_writer(tmp_path):
+    img = np.zeros((2, 3, 3), np.float32)
+    img[0, 0] = [1, 0.5, 0]
+    img[1, 2] = [2, -1, 0.25]
+    p = tmp_path / "a.ppm"
+    S.write_ppm(p, img)
+    t = p.read_text().split()
+    assert t[:4] == ["P3", "3", "2", "255"]
+    v = np.array(t[4:], int).reshape(2, 3, 3)
+    assert np.array_equal(v, srgb8(img))
+
+
+def test_xml_errors(tmp_path):
+    L = S._setup()
+    h = C.c_void_p()
+    assert L.ckr_xml_load(b"/nonexistent.xml", C.byref(h)) == -9
+    bad = tmp_path / "bad.xml"
+    bad.write_text("<SCREEN><WIDTH>4</WIDTH></SCREEN>")
+    assert L.ckr_xml_load(str(bad).encode(), C.byref(h)) == -8
+    bad.write_text("<SCREEN><WIDTH>4</WIDTH><HEIGHT>4")
+    assert L.ckr_xml_load(str(bad).encode(), C.byref(h)) == -8

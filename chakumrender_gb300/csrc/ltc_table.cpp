@@ -122,6 +122,26 @@ extern "C" int ckr_ltc_init(const char *table_path) {
   return st;
 }
 
+// Host-only replay of the renderer's FP32 BRDF and pdf (brdf_eval / pdf_eval of
+// shading_device.cuh), for the CPU test suite: vectors are 3 floats per row.
+// Not part of the public ABI and not used by any product entry point.
+extern "C" int ckr_internal_brdf_host(const ckr_material *mats, uint32_t count, const float *n, const float *wo_ref,
+                                      const float *wo, const float *wi, float *brdf, float *pdf) {
+  for (uint32_t i = 0; i < count; ++i) {
+    ckr::Material m;
+    m.brdf = mats[i].brdf;
+    m.alpha = mats[i].alpha;
+    m.phong_exp = mats[i].phong_exp;
+    m.spec = mats[i].spec;
+    m.int_ior = mats[i].int_ior;
+    m.ext_ior = mats[i].ext_ior;
+    auto v = [&](const float *p) { return ckr::f3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); };
+    brdf[i] = ckr::brdf_eval(m, v(n), v(wo_ref), v(wo), v(wi));
+    pdf[i] = ckr::pdf_eval(m, v(n), v(wo_ref), v(wo), v(wi));
+  }
+  return CKR_OK;
+}
+
 // Host-only replay of ckr_ltc_shade's per-pixel FP32 code (the same functions
 // from shading_device.cuh compiled for the host), for the CPU test suite.  Not
 // part of the public ABI and not used by any product entry point.

@@ -57,19 +57,27 @@ SHD float fresnel(const Material &m, float c) {
   tmp *= tmp;
   return F * 0.5f * tmp;
 }
+// tan^2 of the angle between unit vectors v and n.  The reference computes
+// 1/cos^2 - 1 (FP64); in FP32 that cancels near cos = 1, which for the
+// near-mirror roughness of its scenes (alpha 5e-4) moves D by tens of percent.
+// |v x n|^2 / cos^2 is the same quantity without the cancellation.
+SHD float tan2_of(F3 v, F3 n) {
+  float c = dot(v, n);
+  F3 s = cross(v, n);
+  return dot(s, s) / (c * c);
+}
+
 SHD float ggx_dist(float alpha, F3 h, F3 n) {
   float cs = dot(h, n);
   cs *= cs;
-  float ts = 1.0f / cs - 1.0f;
+  float ts = tan2_of(h, n);
   float as = alpha * alpha;
   ts += as;
   ts *= ts;
   return as / (kPi * cs * cs * ts);
 }
 SHD float ggx_g1(float alpha, F3 v, F3 h, F3 n) {
-  float cs = dot(v, n);
-  cs *= cs;
-  float ts = 1.0f / cs - 1.0f;
+  float ts = tan2_of(v, n);
   if (ts <= 1e-15f) return 1.0f;
   if (dot(h, v) <= 1e-15f) return 0.0f;
   ts = ts * (alpha * alpha) + 1.0f;
@@ -78,7 +86,7 @@ SHD float ggx_g1(float alpha, F3 v, F3 h, F3 n) {
 SHD float beckmann_dist(float alpha, F3 h, F3 n) {
   float cs = dot(h, n);
   cs *= cs;
-  float ts = 1.0f / cs - 1.0f;
+  float ts = tan2_of(h, n);
   float as = alpha * alpha;
   return expf(-ts / as) / (kPi * cs * cs * as);
 }
@@ -88,7 +96,7 @@ SHD float beckmann_g1(float alpha, F3 v, F3 h, F3 n) {
   cs *= cs;
   if (cs >= 0.999999f) return 1.0f;
   if (dot(h, v) <= 1e-15f) return 0.0f;
-  float a = 1.0f / (alpha * sqrtf(1.0f / cs - 1.0f));
+  float a = 1.0f / (alpha * sqrtf(tan2_of(v, n)));
   return a < 1.6f ? rational_g1(a) : 1.0f;
 }
 SHD float phong_g1(float alpha, F3 v, F3 h, F3 n) {
@@ -96,7 +104,7 @@ SHD float phong_g1(float alpha, F3 v, F3 h, F3 n) {
   cs *= cs;
   if (cs >= 0.999999f) return 1.0f;
   if (dot(h, v) <= 1e-15f) return 0.0f;
-  float a = sqrtf((0.5f * alpha + 1.0f) / (1.0f / cs - 1.0f));
+  float a = sqrtf((0.5f * alpha + 1.0f) / tan2_of(v, n));
   return a < 1.6f ? rational_g1(a) : 1.0f;
 }
 SHD float phong_dist(float alpha, F3 h, F3 n) { return (alpha + 2.0f) * powf(dot(h, n), alpha) / (2.0f * kPi); }
@@ -326,6 +334,15 @@ SHD float edge_factor(F3 v1, F3 v2) {
 SHD float integrate_edge(F3 v1, F3 v2, F3 n) { return dot(cross(v1, v2), n) * edge_factor(v1, v2); }
 SHD float integrate_edge_z(F3 v1, F3 v2) { return (v1.x * v2.y - v1.y * v2.x) * edge_factor(v1, v2); }
 
+// Edge crossing test of clipTriangle.  The reference intersects edge PQ with the
+// plane at i = P + (P - Q) d and accepts it when (i - P).(Q - i) > 0 (for edge CA
+// it compares x coordinates only, :101-102).  Since i - P = (P - Q) d and
+// Q - i = (Q - P)(1 + d), that product is -|P - Q|^2 d (1 + d) (x only for CA),
+// positive exactly when -1 < d < 0 (and, for CA, A.x != C.x).  Testing d
+// directly gives the same answer without the cancellation that makes the
+// product round to zero in FP32 when a vertex lies within ~1e-4 of the plane.
+SHD bool edge_crossed(float d) { return d > -1.0f && d < 0.0f; }
+
 // Records a clipped edge segment: the first two points go to q0, q1, the next
 // two to q2, q3 (clipTriangle's clip[idx++] sequence without a local array).
 struct Clip4 {
@@ -354,8 +371,9 @@ SHD bool clip_triangle(F3 A, F3 B, F3 C, F3 n, F3 P, float nA, float nB, float n
   float nAB = dot(n, dAB), nBC = dot(n, dBC), nCA = dot(n, dCA);
   float pA = dot(n, P - A), pB = dot(n, P - B), pC = dot(n, P - C);
   if (nAB * nAB > eps) {
-    F3 i = dAB * (pA / nAB) + A;
-    if (dot(i - A, B - i) > 0.f) {
+    float d = pA / nAB;
+    F3 i = dAB * d + A;
+    if (edge_crossed(d)) {
       ++hits;
       if (nA < 0.f) clip.push(i, B);
       else clip.push(A, i);
@@ -364,8 +382,9 @@ SHD bool clip_triangle(F3 A, F3 B, F3 C, F3 n, F3 P, float nA, float nB, float n
     return false;
   }
   if (nBC * nBC > eps) {
-    F3 i = dBC * (pB / nBC) + B;
-    if (dot(i - B, C - i) > 0.f) {
+    float d = pB / nBC;
+    F3 i = dBC * d + B;
+    if (edge_crossed(d)) {
       ++hits;
       if (nB < 0.f) clip.push(i, C);
       else clip.push(B, i);
@@ -374,8 +393,9 @@ SHD bool clip_triangle(F3 A, F3 B, F3 C, F3 n, F3 P, float nA, float nB, float n
     return false;
   }
   if (nCA * nCA > eps) {
-    F3 i = dCA * (pC / nCA) + C;
-    if ((i.x - C.x) * (A.x - i.x) > 0.f) {
+    float d = pC / nCA;
+    F3 i = dCA * d + C;
+    if (edge_crossed(d) && A.x != C.x) {
       ++hits;
       if (nC < 0.f) clip.push(i, A);
       else clip.push(C, i);
@@ -393,8 +413,9 @@ SHD bool clip_triangle_z(F3 A, F3 B, F3 C, float nA, float nB, float nC, Clip4 &
   clip.idx = 0;
   F3 dAB = A - B, dBC = B - C, dCA = C - A;
   if (dAB.z * dAB.z > eps) {
-    F3 i = dAB * (-A.z / dAB.z) + A;
-    if (dot(i - A, B - i) > 0.f) {
+    float d = -A.z / dAB.z;
+    F3 i = dAB * d + A;
+    if (edge_crossed(d)) {
       ++hits;
       if (nA < 0.f) clip.push(i, B);
       else clip.push(A, i);
@@ -403,8 +424,9 @@ SHD bool clip_triangle_z(F3 A, F3 B, F3 C, float nA, float nB, float nC, Clip4 &
     return false;
   }
   if (dBC.z * dBC.z > eps) {
-    F3 i = dBC * (-B.z / dBC.z) + B;
-    if (dot(i - B, C - i) > 0.f) {
+    float d = -B.z / dBC.z;
+    F3 i = dBC * d + B;
+    if (edge_crossed(d)) {
       ++hits;
       if (nB < 0.f) clip.push(i, C);
       else clip.push(B, i);
@@ -413,8 +435,9 @@ SHD bool clip_triangle_z(F3 A, F3 B, F3 C, float nA, float nB, float nC, Clip4 &
     return false;
   }
   if (dCA.z * dCA.z > eps) {
-    F3 i = dCA * (-C.z / dCA.z) + C;
-    if ((i.x - C.x) * (A.x - i.x) > 0.f) {
+    float d = -C.z / dCA.z;
+    F3 i = dCA * d + C;
+    if (edge_crossed(d) && A.x != C.x) {
       ++hits;
       if (nC < 0.f) clip.push(i, A);
       else clip.push(C, i);

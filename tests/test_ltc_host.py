@@ -40,9 +40,11 @@ def host_replay(g, lt, lc):
 
 
 def ltc_errors(got, ref):
-    """Per-pixel error relative to the pixel's own magnitude (floored at 1e-3 of the
-    image mean, below which a pixel carries no visible energy)."""
-    mag = np.maximum(np.abs(ref).max(axis=1), 1e-3 * np.abs(ref).mean())
+    """Per-pixel error relative to the pixel's own magnitude, floored at 1% of the image
+    mean: pixels darker than that (emitters at grazing angles, where the polygon
+    integral is a small difference of larger edge terms) are held to an absolute error
+    of 1e-4 x 1% of the mean instead."""
+    mag = np.maximum(np.abs(ref).max(axis=1), 1e-2 * np.abs(ref).mean())
     return np.abs(got - ref).max(axis=1) / mag
 
 
@@ -69,6 +71,15 @@ def test_oracle_matches_live_reference():
     a = O.ltc_shade_batch(m, g[:, 0:3], g[:, 4:7], g[:, 8:11], lt, lc)
     b = O.ltc_shade_batch(m, g[:, 0:3], g[:, 4:7], g[:, 8:11], lt, lc, reference=True)
     assert np.array_equal(a, b)
+
+
+@pytest.mark.slow
+def test_fp32_ltc_replay_full_size():
+    """All 1024^2 pixels of the benchmark G-buffer (about 8 s of CPU)."""
+    g = ckr.gbuffer(2, 1024 * 1024)
+    lt, lc = ckr.quad_lights(3, 8)
+    err = ltc_errors(host_replay(g, lt, lc), oracle_ltc(g, lt, lc))
+    assert err.max() <= 1e-4, np.sort(err)[-10:]
 
 
 def test_fp32_ltc_replay_vs_oracle():

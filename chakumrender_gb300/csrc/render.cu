@@ -559,3 +559,159 @@ extern "C" int ckr_render_host(ckr_scene *s, const ckr_camera *cam, const ckr_re
   }
   return st;
 }
+
+// ---- rendering from a static arena (no device allocation) -------------------
+//
+// For callers that may not allocate device memory while they render: code that
+// runs during CUDA stream capture (cudaMalloc / cudaFree are not capturable and
+// may synchronise the device), frame loops that cannot afford the implicit
+// synchronisation of an allocation, and hosts whose device memory is owned by
+// their own allocator.  ckr_render_noalloc runs the same kernels as ckr_render,
+// but its scratch memory (path state, path and shadow-ray queues, FP64 sums,
+// a copy of the LTC table) lives in file-scope device arrays that every GPU
+// loading the library holds until the process exits.
+namespace ckr {
+namespace {
+
+constexpr uint32_t kNoAllocWave = 32768;         // paths per wave
+constexpr uint32_t kNoAllocShadow = 131072;      // shadow rays per wave
+constexpr uint32_t kNoAllocMaxPixels = 262144;   // output pixels (512 x 512)
+constexpr size_t kNoAllocArenaBytes = 16u << 20;  // 16 MiB
+
+constexpr size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t kPathBytes = 4 * a256(16ull * kNoAllocWave) + 4 * a256(4ull * kNoAllocWave);
+constexpr size_t kShadowBytes = 3 * a256(16ull * kNoAllocShadow) + a256(4ull * kNoAllocShadow);
+constexpr size_t kAccumBytes = a256(24ull * kNoAllocMaxPixels);
+static_assert(kPathBytes + kShadowBytes + 2 * 256 + kAccumBytes <= kNoAllocArenaBytes, "arena too small");
+
+static __device__ __align__(256) unsigned char g_noalloc_arena[kNoAllocArenaBytes];
+static __device__ __align__(256) LtcEntry g_noalloc_ltc[4096];
+
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_arena_dev[64] = {};
+LtcEntry *g_noalloc_ltc_dev[64] = {};
+
+// Once per device, with that device current: the arrays' device addresses
+// (the host-side names are only stand-ins) and the LTC table upload.
+int noalloc_setup(int dev) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (g_noalloc_arena_dev[dev]) return CKR_OK;
+  std::vector<LtcEntry> table;
+  int st = load_ltc_table(nullptr, table);
+  if (st != CKR_OK) return st;
+  void *arena = nullptr, *ltc = nullptr;
+  CKR_CUDA_TRY(cudaGetSymbolAddress(&arena, g_noalloc_arena));
+  CKR_CUDA_TRY(cudaGetSymbolAddress(&ltc, g_noalloc_ltc));
+  CKR_CUDA_TRY(cudaMemcpy(ltc, table.data(), table.size() * sizeof(LtcEntry), cudaMemcpyHostToDevice));
+  g_noalloc_ltc_dev[dev] = static_cast<LtcEntry *>(ltc);
+  g_noalloc_arena_dev[dev] = static_cast<unsigned char *>(arena);
+  return CKR_OK;
+}
+
+}  // namespace
+}  // namespace ckr
+
+extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb,
+                                  void *stream_) {
+  if (!s || !cam || !cfg || !rgb || cam->width == 0 || cam->height == 0 || cfg->spp == 0 || cfg->shader > 2)
+    return CKR_ERR_INVALID_ARGUMENT;
+  if (!s->has_shading) return CKR_ERR_INVALID_ARGUMENT;
+  if (cfg->max_depth > 60 || cfg->spp > 65536 || cfg->n_light_samples > 256 || cfg->n_brdf_samples > 256)
+    return CKR_ERR_TOO_LARGE;
+  if ((uint64_t)cam->width * cam->height > kNoAllocMaxPixels) return CKR_ERR_TOO_LARGE;
+  cudaStream_t stream = (cudaStream_t)stream_;
+  int dev = 0;
+  CKR_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return CKR_ERR_INVALID_ARGUMENT;
+  int st = noalloc_setup(dev);
+  if (st != CKR_OK) return st;
+  Params prm;
+  prm.shader = cfg->shader;
+  prm.spp = cfg->spp;
+  prm.max_depth = cfg->shader == CKR_SHADER_PATH ? std::max(1u, cfg->max_depth) : 1u;
+  prm.n_light = cfg->n_light_samples;
+  prm.n_brdf = cfg->shader == CKR_SHADER_PATH ? 1u : cfg->n_brdf_samples;
+  prm.rr_prob = cfg->shader == CKR_SHADER_PATH ? cfg->rr_prob : 0.f;
+  prm.seed = cfg->seed;
+  prm.npix = cam->width * cam->height;
+  uint32_t area_lights = 0, point_lights = 0;
+  for (const DevLight &L : s->host_lights) (L.type == CKR_LIGHT_POINT ? point_lights : area_lights)++;
+  uint64_t per_path = (uint64_t)point_lights + (uint64_t)area_lights * prm.n_light +
+                      (cfg->shader == CKR_SHADER_DIRECT_MIS ? prm.n_brdf : 0);
+  if (per_path > kNoAllocShadow) return CKR_ERR_TOO_LARGE;
+  prm.shadow_per_path = (uint32_t)std::max<uint64_t>(1, per_path);
+  uint64_t total = (uint64_t)prm.npix * prm.spp;
+  uint32_t wave = (uint32_t)std::min<uint64_t>(total, std::min<uint64_t>(kNoAllocWave, kNoAllocShadow / prm.shadow_per_path));
+  // Carve the arena.
+  unsigned char *p = g_noalloc_arena_dev[dev];
+  auto take = [&](size_t bytes) {
+    unsigned char *r = p;
+    p += a256(bytes);
+    return r;
+  };
+  Paths P;
+  P.ray_o = reinterpret_cast<float4 *>(take(16ull * kNoAllocWave));
+  P.ray_d = reinterpret_cast<float4 *>(take(16ull * kNoAllocWave));
+  P.beta = reinterpret_cast<float4 *>(take(16ull * kNoAllocWave));
+  P.meta = reinterpret_cast<uint4 *>(take(16ull * kNoAllocWave));
+  P.hit_id = reinterpret_cast<uint32_t *>(take(4ull * kNoAllocWave));
+  P.hit_t = reinterpret_cast<float *>(take(4ull * kNoAllocWave));
+  P.q0 = reinterpret_cast<uint32_t *>(take(4ull * kNoAllocWave));
+  P.q1 = reinterpret_cast<uint32_t *>(take(4ull * kNoAllocWave));
+  P.sh_o = reinterpret_cast<float4 *>(take(16ull * kNoAllocShadow));
+  P.sh_d = reinterpret_cast<float4 *>(take(16ull * kNoAllocShadow));
+  P.sh_c = reinterpret_cast<float4 *>(take(16ull * kNoAllocShadow));
+  P.sh_px = reinterpret_cast<uint32_t *>(take(4ull * kNoAllocShadow));
+  P.counts = reinterpret_cast<uint32_t *>(take(16));
+  P.stats = reinterpret_cast<unsigned long long *>(take(16));
+  P.accum = reinterpret_cast<double *>(take(24ull * kNoAllocMaxPixels));
+  // The arena keeps the previous call's contents: clear what must start at zero.
+  CKR_CUDA_TRY(cudaMemsetAsync(P.counts, 0, 16, stream));
+  CKR_CUDA_TRY(cudaMemsetAsync(P.stats, 0, 16, stream));
+  CKR_CUDA_TRY(cudaMemsetAsync(P.accum, 0, sizeof(double) * 3 * (size_t)prm.npix, stream));
+  Cam c;
+  c.pos = f3(cam->pos[0], cam->pos[1], cam->pos[2]);
+  c.dir = f3(cam->dir[0], cam->dir[1], cam->dir[2]);
+  c.cx = f3(cam->cx[0], cam->cx[1], cam->cx[2]);
+  c.cy = f3(cam->cy[0], cam->cy[1], cam->cy[2]);
+  c.w = cam->width;
+  c.h = cam->height;
+  SceneView sv = view_of(s);
+  ShadeView shv = shade_view_of(s);
+  const LtcEntry *ltc = g_noalloc_ltc_dev[dev];
+  int depth = (int)stack_depth_of(s);
+  size_t smem = (size_t)depth * kRTPB * sizeof(int32_t);
+  if (smem > 48 * 1024) {
+    CKR_CUDA_TRY(cudaFuncSetAttribute(k_extend, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CKR_CUDA_TRY(cudaFuncSetAttribute(k_shadow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
+  const int g_ext = grid_for((const void *)k_extend, smem, kRTPB);
+  const int g_sh = grid_for((const void *)k_shadow, smem, kRTPB);
+  const void *shade_fn = cfg->shader == CKR_SHADER_PATH ? (const void *)k_shade<CKR_SHADER_PATH>
+                         : cfg->shader == CKR_SHADER_DIRECT_MIS ? (const void *)k_shade<CKR_SHADER_DIRECT_MIS>
+                                                                : (const void *)k_shade<CKR_SHADER_DIRECT_MISCV>;
+  const int g_shade = grid_for(shade_fn, 0, kRTPB);
+  for (uint64_t base = 0; base < total; base += wave) {
+    uint32_t n = (uint32_t)std::min<uint64_t>(wave, total - base);
+    k_camera<<<std::min<int>(g_ext, ceil_div(n, kRTPB)), kRTPB, 0, stream>>>(c, P, prm, base, n);
+    int cur = 0;
+    for (uint32_t d = 0; d <= prm.max_depth; ++d) {
+      k_extend<<<g_ext, kRTPB, smem, stream>>>(sv, P, cur, depth);
+      CKR_CUDA_TRY(cudaMemsetAsync(P.counts + (cur ^ 1), 0, sizeof(uint32_t), stream));
+      CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), stream));
+      if (cfg->shader == CKR_SHADER_PATH)
+        k_shade<CKR_SHADER_PATH><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
+      else if (cfg->shader == CKR_SHADER_DIRECT_MIS)
+        k_shade<CKR_SHADER_DIRECT_MIS><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
+      else
+        k_shade<CKR_SHADER_DIRECT_MISCV><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
+      k_shadow<<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur);
+      cur ^= 1;
+      if (cfg->shader != CKR_SHADER_PATH) break;
+    }
+  }
+  uint32_t n3 = prm.npix * 3;
+  k_resolve<<<std::min<unsigned>(1024, ceil_div(n3, 256)), 256, 0, stream>>>(P.accum, rgb, n3, 1.0 / prm.spp);
+  CKR_CUDA_TRY(cudaGetLastError());
+  return CKR_OK;
+}

@@ -209,6 +209,24 @@ typedef struct ckr_render_cfg {
 int ckr_render(ckr_scene *scene, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb, double *accum,
                void *stream);
 
+/* Rendering that allocates no device memory.  No counterpart in the reference:
+ * it exists for callers that must not allocate while they render, such as code
+ * running inside CUDA stream capture (cudaMalloc / cudaFree cannot be captured
+ * and may synchronise the device), frame loops that cannot take an allocation's
+ * implicit synchronisation, and hosts whose device memory belongs to their own
+ * allocator.  Same result as ckr_render with accum = NULL (up to the order of
+ * the FP64 sums); the scene must already exist.  All scratch memory (path
+ * state, queues, shadow rays, FP64 sums, an LTC table copy) lives in one
+ * static device arena of 16 MiB plus 192 KiB, which every GPU that loads the
+ * library holds until the process exits.  Limits: width * height <= 262144
+ * pixels and <= 131072 shadow rays per path sample, else CKR_ERR_TOO_LARGE.
+ * The first call on a device looks up the arena's device address and uploads
+ * the LTC table with synchronous copies: make that first call before any
+ * stream capture.  Every call uses the same arena, so calls that overlap on
+ * the GPU (other streams or host threads) race: serialise them. */
+int ckr_render_noalloc(ckr_scene *scene, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb,
+                       void *stream);
+
 /* Rays traced by ckr_render on this scene since the last reset: closest-hit
  * rays (camera + continuation) and shadow rays.  Synchronises the device. */
 int ckr_render_stats(ckr_scene *scene, uint64_t *closest_rays, uint64_t *shadow_rays, int reset);

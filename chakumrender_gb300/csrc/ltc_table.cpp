@@ -142,6 +142,39 @@ extern "C" int ckr_internal_brdf_host(const ckr_material *mats, uint32_t count, 
   return CKR_OK;
 }
 
+// Host-only replay of the renderer's FP32 LTC-approximate BRDF (the
+// `brdfApprox.isSet` branch of MaterialType::brdf after getBrdfApproxParam with
+// force, as the MISCV residual uses it); GGX materials only.  For tests.
+extern "C" int ckr_internal_brdf_ltc_host(const ckr_material *mats, uint32_t count, const float *n, const float *wo,
+                                          const float *wi, float *brdf) {
+  std::vector<ckr::LtcEntry> tab;
+  {
+    std::lock_guard<std::mutex> lock(ckr::g_mu);
+    if (ckr::g_host.empty()) {
+      int st = ckr::load_ltc_table(nullptr, ckr::g_host);
+      if (st != CKR_OK) return st;
+    }
+    tab = ckr::g_host;
+  }
+  auto table = [&](int i) { return tab[i]; };
+  for (uint32_t i = 0; i < count; ++i) {
+    ckr::Material m;
+    m.brdf = mats[i].brdf;
+    m.alpha = mats[i].alpha;
+    m.phong_exp = mats[i].phong_exp;
+    m.spec = mats[i].spec;
+    m.int_ior = mats[i].int_ior;
+    m.ext_ior = mats[i].ext_ior;
+    auto v = [&](const float *p) { return ckr::f3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); };
+    ckr::F3 N = v(n), O = v(wo), I = v(wi);
+    float theta = acosf(fminf(1.0f, fmaxf(-1.0f, ckr::dot(N, O))));
+    ckr::LtcLookup L = ckr::ltc_lookup(table, theta, m.alpha);
+    ckr::M3f minv = ckr::ltc_minv_world(L, N, O);
+    brdf[i] = ckr::brdf_ltc(m, L, minv, N, I);
+  }
+  return CKR_OK;
+}
+
 // Host-only replay of ckr_ltc_shade's per-pixel FP32 code (the same functions
 // from shading_device.cuh compiled for the host), for the CPU test suite.  Not
 // part of the public ABI and not used by any product entry point.

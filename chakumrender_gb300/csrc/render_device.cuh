@@ -54,7 +54,7 @@ __device__ __forceinline__ Surface make_surface(const ShadeView &sv, F3 o, F3 d,
     F3 A = f3(__ldg(t9), __ldg(t9 + 1), __ldg(t9 + 2));
     F3 B = f3(__ldg(t9 + 3), __ldg(t9 + 4), __ldg(t9 + 5));
     F3 C = f3(__ldg(t9 + 6), __ldg(t9 + 7), __ldg(t9 + 8));
-    n = normalize(cross(C - A, B - A));
+    n = normalize(cross_rn(C - A, B - A));
     s.mat = __ldg(&sv.tri_mat[id]);
   }
   if (dot(d, n) > 0.f) n = -n;
@@ -104,7 +104,7 @@ __device__ __forceinline__ F3 tri_normal(const ShadeView &sv, uint32_t id) {
   F3 A = f3(__ldg(t9), __ldg(t9 + 1), __ldg(t9 + 2));
   F3 B = f3(__ldg(t9 + 3), __ldg(t9 + 4), __ldg(t9 + 5));
   F3 C = f3(__ldg(t9 + 6), __ldg(t9 + 7), __ldg(t9 + 8));
-  return normalize(cross(C - A, B - A));
+  return normalize(cross_rn(C - A, B - A));
 }
 
 __device__ __forceinline__ F3 mat_radiance(const ShadeView &sv, uint32_t m) {

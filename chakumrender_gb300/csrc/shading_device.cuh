@@ -29,6 +29,18 @@ SHD F3 operator*(F3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
 SHD F3 operator-(F3 a) { return f3(-a.x, -a.y, -a.z); }
 SHD float dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 SHD F3 cross(F3 a, F3 b) { return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+// Cross product with separately rounded products (no fused multiply-add): a
+// component whose two products are equal comes out exactly zero, as in the
+// reference's arithmetic.  Geometric normals use it because ref_frame branches
+// on n.x != 0, so a rounding residue there would rotate the sampling frame.
+SHD F3 cross_rn(F3 a, F3 b) {
+#if defined(__CUDA_ARCH__)
+  return f3(__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y)), __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z)),
+            __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+#else
+  return cross(a, b);  // host code is built without contraction
+#endif
+}
 SHD float length(F3 a) { return sqrtf(dot(a, a)); }
 SHD F3 normalize(F3 a) { return a * (1.0f / sqrtf(dot(a, a))); }
 SHD F3 mulc(F3 a, F3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }

@@ -53,9 +53,12 @@ def test_reference_scenes_vs_oracle(torch_cuda, name, shader):
     o = O.render(sd, sd.camera, cfg)
     e = rel_mse(g, o)
     print(f"{name}: relMSE vs oracle {e:.3e}")
-    # scene0 holds near-mirror plates (GGX alpha 5e-4): FP32 vs FP64 perturbs the few
-    # samples that land in their lobes, so its bar is looser than scene1's.
-    assert e <= (1e-3 if name == "scene0" else 1e-4)
+    # FP32 against FP64 with the same random streams: the images agree sample by
+    # sample, so the bar is far below 1-spp noise (measured 1.3e-7 and 2.8e-5).
+    # scene0's tilted plates have normals with an exactly zero x component, which
+    # picks ref_frame's second branch; a fused cross product would leave a residue
+    # there, rotate every BRDF sample's frame and cost relMSE ~1.
+    assert e <= 1e-4
     mean, p99 = block_agreement(g, srgb8(o).astype(np.uint8))
     assert mean <= 0.01 and p99 <= 0.1, (mean, p99)
 

@@ -237,8 +237,32 @@ def bench_ltc(torch, steps: int):
     b.record(stream)
     torch.cuda.synchronize()
     sec = a.elapsed_time(b) / 1e3 / k
+    # Against the 4096-spp Monte Carlo reference of the same integral (FP64 sums).
+    ltc = out.double()
+    mc = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    mc2 = torch.empty_like(mc)
+    a.record(stream)
+    ckr.ltc_mc(g.data_ptr(), n, dt.data_ptr(), dc.data_ptr(), len(lt), 4096, 1, False, mc.data_ptr(),
+               stream.cuda_stream)
+    b.record(stream)
+    ckr.ltc_mc(g.data_ptr(), n, dt.data_ptr(), dc.data_ptr(), len(lt), 4096, 2, False, mc2.data_ptr(),
+               stream.cuda_stream)
+    torch.cuda.synchronize()
+    mc_ms = a.elapsed_time(b)
+
+    def rel_mse(x, y):
+        return float(((x - y) ** 2 / (y * y + 1e-2)).mean())
+
+    mc_f = torch.empty_like(mc)
+    ckr.ltc_mc(g.data_ptr(), n, dt.data_ptr(), dc.data_ptr(), len(lt), 4096, 1, True, mc_f.data_ptr(),
+               stream.cuda_stream)
+    torch.cuda.synchronize()
     return {"workload": "LTC shading, 1024x1024 G-buffer, 8 quad lights", "ms_per_frame": round(1e3 * sec, 4),
-            "mpixels_per_s": round(n / sec / 1e6, 1), "io_gb_per_s": round(n * 60 / sec / 1e9, 1)}
+            "mpixels_per_s": round(n / sec / 1e6, 1), "io_gb_per_s": round(n * 60 / sec / 1e9, 1),
+            "vs_mc_4096spp": {"relmse_ltc_vs_mc": round(rel_mse(ltc, mc), 6),
+                              "relmse_ltc_vs_mc_with_fresnel": round(rel_mse(ltc, mc_f), 6),
+                              "relmse_mc_seed_to_seed": round(rel_mse(mc2, mc), 7),
+                              "mc_ms": round(mc_ms, 2)}}
 
 
 def cpu_side_baselines(tri_unused=None):

@@ -73,6 +73,7 @@ def lib() -> C.CDLL:
     _sig(L, "ckr_rng_uniform", [C.c_uint64, C.c_uint64, U32], F32)
     _sig(L, "ckr_ltc_init", [C.c_char_p])
     _sig(L, "ckr_ltc_shade", [P, U32, P, P, U32, P, P])
+    _sig(L, "ckr_ltc_mc", [P, U32, P, P, U32, U32, C.c_uint64, C.c_int, P, P])
     _sig(L, "ckr_workload_gbuffer", [C.c_uint64, U32, P])
     _sig(L, "ckr_workload_quad_lights", [C.c_uint64, U32, F32, F32, F32, P, P])
     _lib = L
@@ -96,6 +97,13 @@ def quad_lights(seed: int, nquads: int = 8, side_lo: float = 0.2, side_hi: float
 def ltc_shade(gbuf_dev: int, npx: int, light_tri_dev: int, light_rgb_dev: int, nlight: int, rgb_dev: int,
               stream: int = 0) -> None:
     check(lib().ckr_ltc_shade(gbuf_dev, npx, light_tri_dev, light_rgb_dev, nlight, rgb_dev, stream), "ckr_ltc_shade")
+
+
+def ltc_mc(gbuf_dev: int, npx: int, light_tri_dev: int, light_rgb_dev: int, nlight: int, spp: int, seed: int,
+           fresnel: bool, rgb_dev: int, stream: int = 0) -> None:
+    """Monte Carlo reference of the LTC integral (device buffers; rgb: npx x 3 doubles)."""
+    check(lib().ckr_ltc_mc(gbuf_dev, npx, light_tri_dev, light_rgb_dev, nlight, spp, seed, int(fresnel), rgb_dev,
+                           stream), "ckr_ltc_mc")
 
 
 def status_string(status: int) -> str:

@@ -11,6 +11,7 @@
 #include <algorithm>
 
 #include "ckr_internal.h"
+#include "ckr_rng.h"
 #include "ltc_table.h"
 #include "shading_device.cuh"
 
@@ -66,6 +67,123 @@ __global__ void __launch_bounds__(kLtcTPB, 2) k_ltc_shade(const float4 *__restri
   }
 }
 
+// ---- Monte Carlo reference for the LTC integral -----------------------------------
+// Per pixel, the integral over the emitter triangles of brdf x cos x radiance,
+// treating the emitters as the LTC integral does: two-sided and unoccluded, a
+// direction that crosses several emitters collecting each one's radiance.
+// Half of the samples pick an emitter point by area, half sample the BRDF
+// (getBrdfDirectionSampleRandomized); both are weighted by the balance heuristic,
+// f cos L / (n_a p_area(w) + n_b p_brdf(w)) with p_area(w) = sum over the
+// emitters w crosses of t^2 / (A_total |cos_l|).  Sums are FP64 per pixel.
+
+constexpr int kMcTPB = 128;
+constexpr uint32_t kMcMaxLights = 256;
+
+// Two-sided ray/triangle distance (Moller & Trumbore 1997); 0 on a miss.
+__device__ __forceinline__ float emitter_t(F3 o, F3 w, F3 a, F3 e1, F3 e2) {
+  F3 p = cross(w, e2);
+  float det = dot(e1, p);
+  if (fabsf(det) < 1e-20f) return 0.f;
+  float inv = 1.0f / det;
+  F3 tv = o - a;
+  float u = dot(tv, p) * inv;
+  if (u < 0.f || u > 1.f) return 0.f;
+  F3 q = cross(tv, e1);
+  float v = dot(w, q) * inv;
+  if (v < 0.f || u + v > 1.f) return 0.f;
+  float t = dot(e2, q) * inv;
+  return t > 0.f ? t : 0.f;
+}
+
+__global__ void __launch_bounds__(kMcTPB) k_ltc_mc(const float4 *__restrict__ gbuf, uint32_t npx,
+                                                   const float *__restrict__ light_tri9,
+                                                   const float *__restrict__ light_rgb, uint32_t nlight, uint32_t spp,
+                                                   uint64_t seed, int fresnel, double *__restrict__ rgb) {
+  __shared__ float4 s_a[kMcMaxLights], s_e1[kMcMaxLights], s_e2[kMcMaxLights];  // .w: r, g, b
+  __shared__ float4 s_n[kMcMaxLights];  // unit normal, 1 / A_total
+  __shared__ float s_cdf[kMcMaxLights];
+  for (uint32_t k = threadIdx.x; k < nlight; k += kMcTPB) {
+    const float *t = light_tri9 + 9 * (size_t)k;
+    F3 a = f3(t[0], t[1], t[2]), b = f3(t[3], t[4], t[5]), c = f3(t[6], t[7], t[8]);
+    F3 e1 = b - a, e2 = c - a, nn = cross_rn(e1, e2);
+    float len = length(nn);
+    s_a[k] = make_float4(a.x, a.y, a.z, light_rgb[3 * k]);
+    s_e1[k] = make_float4(e1.x, e1.y, e1.z, light_rgb[3 * k + 1]);
+    s_e2[k] = make_float4(e2.x, e2.y, e2.z, light_rgb[3 * k + 2]);
+    F3 un = len > 0.f ? nn * (1.0f / len) : f3(0.f, 0.f, 0.f);
+    s_n[k] = make_float4(un.x, un.y, un.z, 0.f);
+    s_cdf[k] = 0.5f * len;  // area, turned into the CDF below
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float total = 0.f;
+    for (uint32_t k = 0; k < nlight; ++k) total += s_cdf[k];
+    float run = 0.f;
+    for (uint32_t k = 0; k < nlight; ++k) {
+      run += s_cdf[k];
+      s_cdf[k] = run / total;
+      s_n[k].w = 1.0f / total;
+    }
+  }
+  __syncthreads();
+  const uint32_t p = blockIdx.x * kMcTPB + threadIdx.x;
+  if (p >= npx) return;
+  float4 g0 = gbuf[3 * (size_t)p], g1 = gbuf[3 * (size_t)p + 1], g2 = gbuf[3 * (size_t)p + 2];
+  F3 x = f3(g0.x, g0.y, g0.z), n = f3(g1.x, g1.y, g1.z), wo = f3(g2.x, g2.y, g2.z);
+  Material M;
+  M.brdf = kGGX;
+  M.alpha = g0.w;
+  M.phong_exp = 0.f;
+  M.spec = g2.w;
+  float sf = sqrtf(g1.w);
+  M.int_ior = fresnel ? (1.0f + sf) / (1.0f - sf) : 1e5f;
+  M.ext_ior = 1.0f;
+  F3 wo_ref = normalize(n * (2.0f * dot(n, wo)) - wo);
+  const uint64_t key = ckr_key(seed, p);
+  const float half = 0.5f * (float)spp;
+  double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
+  for (uint32_t s = 0; s < spp; ++s) {
+    float e0 = ckr_draw_f(key, 4 * s), e1 = ckr_draw_f(key, 4 * s + 1), e2 = ckr_draw_f(key, 4 * s + 2);
+    F3 w;
+    if ((s & 1u) == 0) {
+      uint32_t k = 0;
+      while (k + 1 < nlight && s_cdf[k] <= e0) ++k;
+      float4 a = s_a[k], u = s_e1[k], v = s_e2[k];
+      F3 A = f3(a.x, a.y, a.z);
+      F3 P = sample_triangle(A, A + f3(u.x, u.y, u.z), A + f3(v.x, v.y, v.z), e1, e2);
+      w = normalize(P - x);
+    } else {
+      w = sample_brdf(M, n, wo_ref, wo, e0, e1, e2);
+    }
+    float c = dot(w, n);
+    if (!(c > 0.f)) continue;
+    float pa = 0.f, L0 = 0.f, L1 = 0.f, L2 = 0.f;
+    for (uint32_t k = 0; k < nlight; ++k) {
+      float4 a = s_a[k], u = s_e1[k], v = s_e2[k];
+      float t = emitter_t(x, w, f3(a.x, a.y, a.z), f3(u.x, u.y, u.z), f3(v.x, v.y, v.z));
+      if (t > 0.f) {
+        float4 un = s_n[k];
+        float cl = fabsf(un.x * w.x + un.y * w.y + un.z * w.z);
+        pa += t * t * un.w / cl;
+        L0 += a.w;
+        L1 += u.w;
+        L2 += v.w;
+      }
+    }
+    if (!(pa > 0.f)) continue;
+    float f = brdf_eval(M, n, wo_ref, wo, w);
+    float pb = pdf_eval(M, n, wo_ref, wo, w);
+    float wgt = f * c / (half * (pa + pb));
+    if (!(wgt < 3.0e38f)) continue;
+    acc0 += (double)(L0 * wgt);
+    acc1 += (double)(L1 * wgt);
+    acc2 += (double)(L2 * wgt);
+  }
+  rgb[3 * (size_t)p] = acc0;
+  rgb[3 * (size_t)p + 1] = acc1;
+  rgb[3 * (size_t)p + 2] = acc2;
+}
+
 }  // namespace
 }  // namespace ckr
 
@@ -93,6 +211,19 @@ extern "C" int ckr_ltc_shade(const float *gbuf, uint32_t npx, const float *light
   int grid = (int)std::min<uint64_t>(ceil_div(npx, kLtcTPB), (uint64_t)sms * per_sm);
   k_ltc_shade<<<grid, kLtcTPB, smem, (cudaStream_t)stream>>>(reinterpret_cast<const float4 *>(gbuf), npx, light_tri9,
                                                                light_rgb, nlight, rgb, table);
+  CKR_CUDA_TRY(cudaGetLastError());
+  return CKR_OK;
+}
+
+extern "C" int ckr_ltc_mc(const float *gbuf, uint32_t npx, const float *light_tri9, const float *light_rgb,
+                          uint32_t nlight, uint32_t spp, uint64_t seed, int fresnel, double *rgb, void *stream) {
+  if ((npx && (!gbuf || !rgb)) || !light_tri9 || !light_rgb || nlight == 0 || ((uintptr_t)gbuf & 15u) ||
+      spp == 0 || (spp & 1u) || spp > (1u << 28))
+    return CKR_ERR_INVALID_ARGUMENT;
+  if (nlight > kMcMaxLights) return CKR_ERR_TOO_LARGE;
+  if (npx == 0) return CKR_OK;
+  k_ltc_mc<<<(unsigned)ceil_div(npx, kMcTPB), kMcTPB, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<const float4 *>(gbuf), npx, light_tri9, light_rgb, nlight, spp, seed, fresnel, rgb);
   CKR_CUDA_TRY(cudaGetLastError());
   return CKR_OK;
 }

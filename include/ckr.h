@@ -271,6 +271,20 @@ int ckr_ltc_init(const char *table_path);
 int ckr_ltc_shade(const float *gbuf, uint32_t npx, const float *light_tri9, const float *light_rgb,
                   uint32_t nlight, float *rgb, void *stream);
 
+/* Monte Carlo estimate of the integral ckr_ltc_shade approximates, per pixel of
+ * the same G-buffer: the integral over the emitter triangles (two-sided and
+ * unoccluded, as the LTC integral treats them) of MaterialType::brdf x cos x
+ * radiance for the GGX material (alpha, spec) of the pixel.  spp samples
+ * (even, >= 2): half pick an emitter point by area, half follow
+ * getBrdfDirectionSampleRandomized; balance-heuristic MIS; FP32 arithmetic,
+ * FP64 per-pixel sums.  fresnel = 0 sets F = 1 (IOR 1e5), the lobe the LTC fit
+ * models; fresnel = 1 takes the IOR from f0: (1 + sqrt f0) / (1 - sqrt f0).
+ * Random numbers: counter 4s..4s+2 of the stream (seed, pixel).  rgb receives
+ * npx x 3 doubles (device).  nlight <= 256 (CKR_ERR_TOO_LARGE above).
+ * No reference counterpart: the LTC's high-spp reference. */
+int ckr_ltc_mc(const float *gbuf, uint32_t npx, const float *light_tri9, const float *light_rgb, uint32_t nlight,
+               uint32_t spp, uint64_t seed, int fresnel, double *rgb, void *stream);
+
 /* ---- synthetic workloads (deterministic; no reference counterpart) ----- */
 /* G-buffer for LTC shading (12 floats per pixel as ckr_ltc_shade reads them):
  * pos uniform in [-1,1]^3, n uniform on the +z hemisphere, v cosine-distributed

@@ -99,6 +99,12 @@ void orc_ltc_shade(const orc_material *m, const double *x3, const double *n3, co
                    const float *light_tri9, const float *light_rgb, uint32_t nlight, double *rgb);
 void orc_ltc_shade_batch(const orc_material *m, uint32_t count, const double *x, const double *n, const double *v,
                          const float *light_tri9, const float *light_rgb, uint32_t nlight, double *rgb, int threads);
+/* Monte Carlo reference for the LTC integral (ckr_ltc_mc of the library in FP64):
+ * spp samples per point (even: emitter area, odd: BRDF), balance heuristic,
+ * random stream (seed, pixel_index[i] or i).  rgb: count x 3 doubles. */
+void orc_ltc_mc(const orc_material *m, uint32_t count, const double *x, const double *n, const double *v,
+                const float *light_tri9, const float *light_rgb, uint32_t nlight, uint32_t spp, uint64_t seed,
+                const uint32_t *pixel_index, double *rgb, int threads);
 /* Renders with the reference's shaders restated in FP64 (see orc_render.inc):
  * desc/cam/cfg are the library's ABI structs (include/ckr.h); rgb receives
  * width*height*3 doubles, top row first, the mean over cfg->spp. */

@@ -51,6 +51,7 @@ def orc() -> C.CDLL:
         _sig(L, "orc_brdf_batch", [P, U32, P, P, P, P, C.c_int, P, P], None)
         _sig(L, "orc_ltc_shade_batch", [P, U32, P, P, P, P, P, U32, P, C.c_int], None)
         _sig(L, "orc_sample_dir", [C.c_int, P, P, C.c_double, C.c_double, C.c_double, P], None)
+        _sig(L, "orc_ltc_mc", [P, U32, P, P, P, P, P, U32, U32, C.c_uint64, P, P, C.c_int], None)
         if L.orc_ltc_load(str(LTC_TABLE).encode()) != 0:
             raise RuntimeError(f"cannot load {LTC_TABLE}")
         _orc = L
@@ -201,6 +202,19 @@ def ltc_shade_batch(mat, x, n, v, light_tri9, light_rgb, reference=False, thread
     out = np.empty((len(mat), 3))
     f = _ref_shading_sigs().ref_ltc_shade_batch if reference else orc().orc_ltc_shade_batch
     f(_p(mat), len(mat), _p(x), _p(n), _p(v), _p(lt), _p(lc), len(lt), _p(out), threads)
+    return out
+
+
+def ltc_mc(mat, x, n, v, light_tri9, light_rgb, spp: int, seed: int, pixel_index=None, threads: int = 0):
+    """FP64 Monte Carlo of the integral the LTC shading approximates (see orc_render.inc)."""
+    mat = np.ascontiguousarray(mat, dtype=MATERIAL)
+    x, n, v = _d3(x), _d3(n), _d3(v)
+    lt = np.ascontiguousarray(light_tri9, dtype=np.float32).reshape(-1, 9)
+    lc = np.ascontiguousarray(light_rgb, dtype=np.float32).reshape(-1, 3)
+    idx = None if pixel_index is None else np.ascontiguousarray(pixel_index, dtype=np.uint32)
+    out = np.empty((len(mat), 3))
+    orc().orc_ltc_mc(_p(mat), len(mat), _p(x), _p(n), _p(v), _p(lt), _p(lc), len(lt), spp, seed,
+                     None if idx is None else _p(idx), _p(out), threads)
     return out
 
 

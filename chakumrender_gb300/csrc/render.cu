@@ -23,6 +23,8 @@
 
 #include "ckr_internal.h"
 #include "ltc_table.h"
+#include "mlp.h"
+#include "proposal.h"
 #include "render_device.cuh"
 
 namespace ckr {
@@ -30,7 +32,19 @@ namespace {
 
 constexpr int kRTPB = 128;
 constexpr uint32_t kCtrDim = 1024;  // counter dims per (sample, vertex)
-constexpr uint32_t kDimBrdf = 1000, kDimRR = 1003;
+constexpr uint32_t kDimBrdf = 1000, kDimRR = 1003, kDimTrain = 1010;
+constexpr uint32_t kNoRec = 0xFFFFFFFFu;
+
+// Hooks of the learned light selection (CKR_SHADER_PATH_NEE with a proposal
+// network); all null for selection in proportion to power.
+struct Learn {
+  const __half *probs;       // [queue row x 64] network output at this bounce's vertices
+  const __half *probs_prev;  // the same at the previous bounce (rows by Paths::prev_row)
+  float delta;               // defensive fraction of the uniform distribution
+  float4 *rec;               // training records, 3 float4 each: (x, alpha), (n, value), (wo, cluster)
+  uint32_t *rec_count;
+  uint32_t rec_cap;
+};
 
 __device__ __forceinline__ uint32_t ctr(uint32_t sample, uint32_t depth, uint32_t dim) {
   return ((sample * 64u + depth) * kCtrDim) + dim;
@@ -56,6 +70,8 @@ struct Paths {
   uint32_t *q0, *q1;  // path-slot queues
   float4 *sh_o, *sh_d, *sh_c;  // shadow rays and their contributions
   uint32_t *sh_px;
+  uint32_t *prev_row;  // learned selection: the path's row in the previous bounce's probabilities
+  uint32_t *sh_rec;    // training: per shadow ray, its training record (kNoRec: none)
   uint32_t *counts;  // [0] q[0] length, [1] q[1] length, [2] shadow count
   unsigned long long *stats;  // cumulative closest-hit rays, shadow rays
   double *accum;     // 3 per output pixel
@@ -127,7 +143,7 @@ __global__ void __launch_bounds__(kRTPB) k_extend(SceneView s, Paths P, int cur,
   }
 }
 
-__global__ void __launch_bounds__(kRTPB) k_shadow(SceneView s, Paths P, int depth, int cur) {
+__global__ void __launch_bounds__(kRTPB) k_shadow(SceneView s, Paths P, int depth, int cur, float4 *rec) {
   extern __shared__ int32_t smem_stack[];
   int32_t *stack = smem_stack + threadIdx.x;
   const uint32_t n = P.counts[2];
@@ -143,6 +159,9 @@ __global__ void __launch_bounds__(kRTPB) k_shadow(SceneView s, Paths P, int dept
     if (trace_ray<true>(s, r, t, stack, kRTPB, depth) == kMiss) {
       float4 c = P.sh_c[i];
       add_px(P.accum, P.sh_px[i], f3(c.x, c.y, c.z));
+    } else if (rec) {
+      uint32_t ri = P.sh_rec[i];
+      if (ri != kNoRec) rec[3 * (size_t)ri + 1].w = 0.f;  // occluded: the sample contributed nothing
     }
   }
 }
@@ -383,6 +402,191 @@ __global__ void __launch_bounds__(kRTPB) k_shade(ShadeView sv, Paths P, Params p
   }
 }
 
+// CKR_SHADER_PATH_NEE: one light sample and one BRDF sample per vertex over many
+// lights.  The light technique draws an emitter light from the selection
+// distribution, one of its triangles in proportion to power and a uniform point
+// on it; the BRDF sample continues the path and, if it meets an emitter, is
+// weighted at the next vertex with the light technique's pdf of the previous
+// vertex (its pdf is carried in beta.w).  Balance heuristic throughout.
+__global__ void __launch_bounds__(kRTPB) k_shade_nee(ShadeView sv, Paths P, Params prm, int cur, Learn lr) {
+  const uint32_t n = P.counts[cur];
+  const uint32_t *q = cur ? P.q1 : P.q0;
+  uint32_t *qn = cur ? P.q0 : P.q1;
+  const int lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (kRTPB / 32);
+  const uint32_t warp_id = blockIdx.x * (kRTPB / 32) + (threadIdx.x >> 5);
+  const float train_frac = lr.rec && n ? fminf(1.0f, (float)lr.rec_cap / (float)n) : 0.f;
+  for (uint32_t base = warp_id * 32; base < n; base += warps * 32) {
+    const uint32_t i = base + lane;
+    const bool valid = i < n;
+    const uint32_t slot = valid ? q[i] : 0;
+    uint32_t nshadow = 0;
+    bool cont = false, rec_ok = false;
+    float4 next_d = make_float4(0, 0, 0, 0), next_b = make_float4(0, 0, 0, 0);
+    float4 so = make_float4(0, 0, 0, 0), sd = so, sc = so, r0 = so, r1 = so, r2 = so;
+    F3 next_o = f3(0, 0, 0);
+    uint4 meta = make_uint4(0, 0, 0, 0);
+    if (valid) {
+      uint32_t id = P.hit_id[slot];
+      meta = P.meta[slot];
+      if (id != kMiss) {
+        float4 ro = P.ray_o[slot], rd = P.ray_d[slot], b4 = P.beta[slot];
+        F3 beta = f3(b4.x, b4.y, b4.z);
+        Surface S = make_surface(sv, f3(ro.x, ro.y, ro.z), f3(rd.x, rd.y, rd.z), id, P.hit_t[slot]);
+        const ckr_material &mm = sv.mats[S.mat];
+        if (mm.light_type != 0) {
+          F3 Le = f3(mm.radiance[0], mm.radiance[1], mm.radiance[2]);
+          if (meta.z == 0) {
+            float mx = Le.x;  // Vec::maxnorm, as the other shaders
+            if (mx < Le.y) mx = Le.y;
+            if (mx < Le.z) mx = Le.z;
+            add_px(P.accum, meta.x, Le * (1.0f / mx));
+          } else {
+            float wb = 1.0f;
+            uint32_t k = (id & kSphereBit) ? kNoLight : __ldg(&sv.tri_light[id]);
+            if (k != kNoLight && b4.w > 0.f) {
+              DevLight L = sv.lights[k];
+              Select sel = make_select(sv, lr.probs_prev ? lr.probs_prev + 64 * (size_t)P.prev_row[slot] : nullptr,
+                                       lr.delta);
+              const float *t9 = sv.tri9 + 9 * (size_t)id;
+              F3 A = f3(__ldg(t9), __ldg(t9 + 1), __ldg(t9 + 2));
+              F3 B = f3(__ldg(t9 + 3), __ldg(t9 + 4), __ldg(t9 + 5));
+              F3 C = f3(__ldg(t9 + 6), __ldg(t9 + 7), __ldg(t9 + 8));
+              F3 nrm = cross_rn(C - A, B - A);
+              float len = length(nrm);
+              float cl = fabsf(dot(nrm, f3(rd.x, rd.y, rd.z))) / len;
+              float pl = nee_pdf(sv, select_prob(sv, sel, k - sv.first_emit), L, id, P.hit_t[slot], 0.5f * len, cl);
+              if (pl > 0.f && pl < 3.0e38f) wb = b4.w / (b4.w + pl);
+            }
+            add_px(P.accum, meta.x, mulc(beta, Le) * wb);
+          }
+        } else if (!(meta.w & 1u)) {
+          Material M = material_of(mm);
+          F3 fcol = f3(mm.color[0], mm.color[1], mm.color[2]) * mm.reflectance;
+          uint64_t key = ckr_key(prm.seed, meta.x);
+          F3 o_off = offset_origin(S.x, S.n);
+          // ---- light technique: one sample ----
+          float e0 = ckr_draw_f(key, ctr(meta.y, meta.z, 0)), e1 = ckr_draw_f(key, ctr(meta.y, meta.z, 1));
+          float e2 = ckr_draw_f(key, ctr(meta.y, meta.z, 2)), e3 = ckr_draw_f(key, ctr(meta.y, meta.z, 3));
+          Select sel = make_select(sv, lr.probs ? lr.probs + 64 * (size_t)i : nullptr, lr.delta);
+          uint32_t j = select_pick(sv, sel, e0);
+          DevLight L = sv.lights[sv.first_emit + j];
+          uint32_t tri = L.first + cdf_pick(sv.pcdf + L.pcdf, L.count, e1);
+          const float *t9 = sv.tri9 + 9 * (size_t)tri;
+          F3 A = f3(__ldg(t9), __ldg(t9 + 1), __ldg(t9 + 2));
+          F3 B = f3(__ldg(t9 + 3), __ldg(t9 + 4), __ldg(t9 + 5));
+          F3 C = f3(__ldg(t9 + 6), __ldg(t9 + 7), __ldg(t9 + 8));
+          F3 Pl = sample_triangle(A, B, C, e2, e3);
+          F3 dv = Pl - S.x;
+          float dist = length(dv);
+          F3 w = dv * (1.0f / dist);
+          float c = dot(w, S.n);
+          F3 nrm = cross_rn(C - A, B - A);
+          float len = length(nrm);
+          float cl = fabsf(dot(nrm, w)) / len;
+          if (c > 0.f && cl > 0.f && len > 0.f && dist > 0.f) {
+            float pl = nee_pdf(sv, select_prob(sv, sel, j), L, tri, dist, 0.5f * len, cl);
+            float f = brdf_eval(M, S.n, S.wo_ref, S.wo, w);
+            if (pl > 0.f && f > 0.f) {
+              float pb = pdf_eval(M, S.n, S.wo_ref, S.wo, w);
+              F3 Le = mat_radiance(sv, sv.tri_mat[tri]);
+              float g = f * c / pl;
+              F3 contrib = mulc(beta, mulc(fcol, Le)) * (g * (pl / (pl + pb)));
+              nshadow = 1;
+              so = make_float4(o_off.x, o_off.y, o_off.z, 0.f);
+              sd = make_float4(w.x, w.y, w.z, shadow_tmax(length(Pl - o_off)));
+              sc = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
+              if (train_frac > 0.f && ckr_draw_f(key, ctr(meta.y, meta.z, kDimTrain)) < train_frac) {
+                // Training sample: the unweighted estimate of cluster j's direct light
+                // (luminance), zeroed by the shadow kernel if the ray is blocked.
+                F3 fl = mulc(fcol, Le);
+                rec_ok = true;
+                r0 = make_float4(S.x.x, S.x.y, S.x.z, M.alpha);
+                r1 = make_float4(S.n.x, S.n.y, S.n.z, (fl.x + fl.y + fl.z) * (1.0f / 3.0f) * g);
+                r2 = make_float4(S.wo.x, S.wo.y, S.wo.z, __uint_as_float(j));
+              }
+            }
+          }
+          // ---- BRDF technique: continues the path ----
+          if (meta.z + 1 <= prm.max_depth) {
+            float b0 = ckr_draw_f(key, ctr(meta.y, meta.z, kDimBrdf));
+            float b1 = ckr_draw_f(key, ctr(meta.y, meta.z, kDimBrdf + 1));
+            float b2 = ckr_draw_f(key, ctr(meta.y, meta.z, kDimBrdf + 2));
+            F3 wn = sample_brdf(M, S.n, S.wo_ref, S.wo, b0, b1, b2);
+            float cn = dot(wn, S.n);
+            float err = ckr_draw_f(key, ctr(meta.y, meta.z, kDimRR));
+            if (cn > 0.f && err >= prm.rr_prob) {
+              float pb = pdf_eval(M, S.n, S.wo_ref, S.wo, wn);
+              float f = brdf_eval(M, S.n, S.wo_ref, S.wo, wn);
+              if (pb > 0.f && f > 0.f) {
+                F3 nb = mulc(beta, fcol) * (f * cn / (pb * (1.0f - prm.rr_prob)));
+                cont = true;
+                next_o = o_off;
+                next_d = make_float4(wn.x, wn.y, wn.z, 3.0e38f);
+                next_b = make_float4(nb.x, nb.y, nb.z, pb);
+              }
+            }
+          }
+        }
+      }
+    }
+    uint32_t rbase = kNoRec;
+    if (lr.rec) {
+      rbase = warp_reserve(lr.rec_count, rec_ok ? 1u : 0u);
+      if (rec_ok && rbase < lr.rec_cap) {
+        lr.rec[3 * (size_t)rbase] = r0;
+        lr.rec[3 * (size_t)rbase + 1] = r1;
+        lr.rec[3 * (size_t)rbase + 2] = r2;
+      } else {
+        rbase = kNoRec;
+      }
+    }
+    uint32_t sbase = warp_reserve(&P.counts[2], nshadow);
+    if (nshadow) {
+      P.sh_o[sbase] = so;
+      P.sh_d[sbase] = sd;
+      P.sh_c[sbase] = sc;
+      P.sh_px[sbase] = meta.x;
+      if (lr.rec) P.sh_rec[sbase] = rbase;
+    }
+    uint32_t cbase = warp_reserve(&P.counts[cur ^ 1], cont ? 1u : 0u);
+    if (cont) {
+      P.ray_o[slot] = make_float4(next_o.x, next_o.y, next_o.z, 0.f);
+      P.ray_d[slot] = next_d;
+      P.beta[slot] = next_b;
+      uint32_t nd = meta.z + 1;
+      P.meta[slot] = make_uint4(meta.x, meta.y, nd, nd >= prm.max_depth ? 1u : 0u);
+      if (lr.probs) P.prev_row[slot] = i;
+      qn[cbase] = slot;
+    }
+  }
+}
+
+// Network input rows of the learned selection, one per queue entry (zeros for
+// entries that are not shaded surfaces).
+__global__ void __launch_bounds__(kRTPB) k_nee_prep(ShadeView sv, Paths P, int cur, float4 *mlp_in) {
+  const uint32_t n = P.counts[cur];
+  const uint32_t *q = cur ? P.q1 : P.q0;
+  for (uint32_t i = blockIdx.x * kRTPB + threadIdx.x; i < n; i += gridDim.x * kRTPB) {
+    const uint32_t slot = q[i], id = P.hit_id[slot];
+    const uint4 meta = P.meta[slot];
+    float4 a = make_float4(0, 0, 0, 0), b = a, c = a;
+    if (id != kMiss && !(meta.w & 1u)) {
+      float4 ro = P.ray_o[slot], rd = P.ray_d[slot];
+      Surface S = make_surface(sv, f3(ro.x, ro.y, ro.z), f3(rd.x, rd.y, rd.z), id, P.hit_t[slot]);
+      const ckr_material &mm = sv.mats[S.mat];
+      if (mm.light_type == 0) {
+        a = make_float4(S.x.x, S.x.y, S.x.z, mm.alpha);
+        b = make_float4(S.n.x, S.n.y, S.n.z, 0.f);
+        c = make_float4(S.wo.x, S.wo.y, S.wo.z, 0.f);
+      }
+    }
+    mlp_in[3 * (size_t)i] = a;
+    mlp_in[3 * (size_t)i + 1] = b;
+    mlp_in[3 * (size_t)i + 2] = c;
+  }
+}
+
 __global__ void k_resolve(const double *accum, float *rgb, uint32_t n3, double inv_spp) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x)
     rgb[i] = (float)(accum[i] * inv_spp);
@@ -415,30 +619,40 @@ namespace {
 void free_ws(void *p) { delete static_cast<Workspace *>(p); }
 }  // namespace
 
-extern "C" int ckr_render(ckr_scene *s, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb, double *accum,
-                          void *stream_) {
-  if (!s || !cam || !cfg || !rgb || cam->width == 0 || cam->height == 0 || cfg->spp == 0 || cfg->shader > 2)
+namespace {
+
+int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb,
+                double *accum, void *stream_) {
+  if (!s || !cam || !cfg || !rgb || cam->width == 0 || cam->height == 0 || cfg->spp == 0 || cfg->shader > 3)
     return CKR_ERR_INVALID_ARGUMENT;
   if (!s->has_shading) return CKR_ERR_INVALID_ARGUMENT;
   if (cfg->max_depth > 60 || cfg->spp > 65536 || cfg->n_light_samples > 256 || cfg->n_brdf_samples > 256)
     return CKR_ERR_TOO_LARGE;
+  if (prop && (cfg->shader != CKR_SHADER_PATH_NEE || prop->net.nclusters != s->n_emit))
+    return CKR_ERR_INVALID_ARGUMENT;
   cudaStream_t stream = (cudaStream_t)stream_;
   std::lock_guard<std::mutex> lock(s->host_mu);
+  std::unique_lock<std::mutex> plock;
+  if (prop) plock = std::unique_lock<std::mutex>(prop->mu);
   int st = CKR_OK;
   const LtcEntry *ltc = device_ltc_table(&st);
   if (!ltc) return st;
   Params prm;
   prm.shader = cfg->shader;
   prm.spp = cfg->spp;
-  prm.max_depth = cfg->shader == CKR_SHADER_PATH ? std::max(1u, cfg->max_depth) : 1u;
+  const bool path = cfg->shader == CKR_SHADER_PATH || cfg->shader == CKR_SHADER_PATH_NEE;
+  if (cfg->shader == CKR_SHADER_PATH_NEE && s->n_emit == 0) return CKR_ERR_INVALID_ARGUMENT;
+  prm.max_depth = path ? std::max(1u, cfg->max_depth) : 1u;
   prm.n_light = cfg->n_light_samples;
-  prm.n_brdf = cfg->shader == CKR_SHADER_PATH ? 1u : cfg->n_brdf_samples;
-  prm.rr_prob = cfg->shader == CKR_SHADER_PATH ? cfg->rr_prob : 0.f;
+  prm.n_brdf = path ? 1u : cfg->n_brdf_samples;
+  prm.rr_prob = path ? cfg->rr_prob : 0.f;
   prm.seed = cfg->seed;
   prm.npix = cam->width * cam->height;
   uint32_t area_lights = 0, point_lights = 0;
   for (const DevLight &L : s->host_lights) (L.type == CKR_LIGHT_POINT ? point_lights : area_lights)++;
-  uint32_t per_path = point_lights + area_lights * prm.n_light + (cfg->shader == CKR_SHADER_DIRECT_MIS ? prm.n_brdf : 0);
+  uint32_t per_path = cfg->shader == CKR_SHADER_PATH_NEE
+                          ? 1u
+                          : point_lights + area_lights * prm.n_light + (cfg->shader == CKR_SHADER_DIRECT_MIS ? prm.n_brdf : 0);
   prm.shadow_per_path = std::max(1u, per_path);
   uint64_t total = (uint64_t)prm.npix * prm.spp;
   size_t wave = (size_t)std::min<uint64_t>(total, std::max<uint64_t>(32768, (1ull << 23) / prm.shadow_per_path));
@@ -472,13 +686,25 @@ extern "C" int ckr_render(ckr_scene *s, const ckr_camera *cam, const ckr_render_
     acc = W.accum.ptr;
   }
   CKR_CUDA_TRY(cudaMemsetAsync(acc, 0, sizeof(double) * 3 * (size_t)prm.npix, stream));
-  Paths P;
+  Paths P{};
   P.ray_o = W.ray_o.ptr; P.ray_d = W.ray_d.ptr; P.beta = W.beta.ptr; P.meta = W.meta.ptr;
   P.hit_id = W.hit_id.ptr; P.hit_t = W.hit_t.ptr; P.q0 = W.q0.ptr; P.q1 = W.q1.ptr;
   P.sh_o = W.sh_o.ptr; P.sh_d = W.sh_d.ptr; P.sh_c = W.sh_c.ptr; P.sh_px = W.sh_px.ptr;
   P.counts = W.counts.ptr;
   P.stats = W.stats.ptr;
   P.accum = acc;
+  const bool train = prop && prop->train;
+  if (prop) {
+    CKR_CUDA_TRY(prop->mlp_in.reserve(3 * wave));
+    CKR_CUDA_TRY(prop->probs[0].reserve(64 * wave));
+    CKR_CUDA_TRY(prop->probs[1].reserve(64 * wave));
+    CKR_CUDA_TRY(prop->prev_row.reserve(wave));
+    CKR_CUDA_TRY(prop->sh_rec.reserve(shadow));
+    CKR_CUDA_TRY(prop->rec.reserve(3 * (size_t)prop->batch));
+    P.prev_row = prop->prev_row.ptr;
+    P.sh_rec = prop->sh_rec.ptr;
+    CKR_CUDA_TRY(cudaMemsetAsync(prop->rec_count.ptr, 0, 4, stream));
+  }
   Cam c;
   c.pos = f3(cam->pos[0], cam->pos[1], cam->pos[2]);
   c.dir = f3(cam->dir[0], cam->dir[1], cam->dir[2]);
@@ -496,7 +722,8 @@ extern "C" int ckr_render(ckr_scene *s, const ckr_camera *cam, const ckr_render_
   }
   const int g_ext = grid_for((const void *)k_extend, smem, kRTPB);
   const int g_sh = grid_for((const void *)k_shadow, smem, kRTPB);
-  const void *shade_fn = cfg->shader == CKR_SHADER_PATH ? (const void *)k_shade<CKR_SHADER_PATH>
+  const void *shade_fn = cfg->shader == CKR_SHADER_PATH_NEE ? (const void *)k_shade_nee
+                         : cfg->shader == CKR_SHADER_PATH      ? (const void *)k_shade<CKR_SHADER_PATH>
                          : cfg->shader == CKR_SHADER_DIRECT_MIS ? (const void *)k_shade<CKR_SHADER_DIRECT_MIS>
                                                                 : (const void *)k_shade<CKR_SHADER_DIRECT_MISCV>;
   const int g_shade = grid_for(shade_fn, 0, kRTPB);
@@ -508,21 +735,62 @@ extern "C" int ckr_render(ckr_scene *s, const ckr_camera *cam, const ckr_render_
       k_extend<<<g_ext, kRTPB, smem, stream>>>(sv, P, cur, depth);
       CKR_CUDA_TRY(cudaMemsetAsync(P.counts + (cur ^ 1), 0, sizeof(uint32_t), stream));
       CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), stream));
-      if (cfg->shader == CKR_SHADER_PATH)
+      Learn lr{};
+      if (prop) {
+        // Network input for this bounce's vertices, then its light distributions.
+        k_nee_prep<<<g_shade, kRTPB, 0, stream>>>(shv, P, cur, prop->mlp_in.ptr);
+        int ms = mlp::infer(prop->net, prop->mlp_in.ptr, (uint32_t)wave, P.counts + cur, prop->probs[d & 1].ptr,
+                            stream);
+        if (ms != CKR_OK) return ms;
+        lr.probs = prop->probs[d & 1].ptr;
+        lr.probs_prev = d ? prop->probs[(d - 1) & 1].ptr : nullptr;
+        lr.delta = prop->defensive;
+        if (train) {
+          lr.rec = prop->rec.ptr;
+          lr.rec_count = prop->rec_count.ptr;
+          lr.rec_cap = prop->batch;
+        }
+      }
+      if (cfg->shader == CKR_SHADER_PATH_NEE)
+        k_shade_nee<<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, lr);
+      else if (cfg->shader == CKR_SHADER_PATH)
         k_shade<CKR_SHADER_PATH><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else if (cfg->shader == CKR_SHADER_DIRECT_MIS)
         k_shade<CKR_SHADER_DIRECT_MIS><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else
         k_shade<CKR_SHADER_DIRECT_MISCV><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
-      k_shadow<<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur);
+      k_shadow<<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur, train ? prop->rec.ptr : nullptr);
+      if (train) {
+        // Adam steps on this bounce's light samples (visibility applied above),
+        // minibatch by minibatch; steps past the records actually written are no-ops.
+        for (uint32_t off = 0; off < prop->batch; off += prop->minibatch) {
+          int ts = mlp::train_step(prop->net, prop->rec.ptr + 3 * (size_t)off,
+                                   std::min(prop->minibatch, prop->batch - off), prop->rec_count.ptr, off, stream);
+          if (ts != CKR_OK) return ts;
+        }
+        CKR_CUDA_TRY(cudaMemsetAsync(prop->rec_count.ptr, 0, 4, stream));
+      }
       cur ^= 1;
-      if (cfg->shader != CKR_SHADER_PATH) break;
+      if (!path) break;
     }
   }
   uint32_t n3 = prm.npix * 3;
   k_resolve<<<std::min<unsigned>(1024, ceil_div(n3, 256)), 256, 0, stream>>>(acc, rgb, n3, 1.0 / prm.spp);
   CKR_CUDA_TRY(cudaGetLastError());
   return CKR_OK;
+}
+
+}  // namespace
+
+extern "C" int ckr_render(ckr_scene *s, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb, double *accum,
+                          void *stream) {
+  return render_impl(s, nullptr, cam, cfg, rgb, accum, stream);
+}
+
+extern "C" int ckr_render_learned(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const ckr_render_cfg *cfg,
+                                  float *rgb, double *accum, void *stream) {
+  if (!prop) return CKR_ERR_INVALID_ARGUMENT;
+  return render_impl(s, prop, cam, cfg, rgb, accum, stream);
 }
 
 extern "C" int ckr_render_stats(ckr_scene *s, uint64_t *closest_rays, uint64_t *shadow_rays, int reset) {
@@ -613,7 +881,7 @@ int noalloc_setup(int dev) {
 
 extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb,
                                   void *stream_) {
-  if (!s || !cam || !cfg || !rgb || cam->width == 0 || cam->height == 0 || cfg->spp == 0 || cfg->shader > 2)
+  if (!s || !cam || !cfg || !rgb || cam->width == 0 || cam->height == 0 || cfg->spp == 0 || cfg->shader > 3)
     return CKR_ERR_INVALID_ARGUMENT;
   if (!s->has_shading) return CKR_ERR_INVALID_ARGUMENT;
   if (cfg->max_depth > 60 || cfg->spp > 65536 || cfg->n_light_samples > 256 || cfg->n_brdf_samples > 256)
@@ -628,16 +896,20 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
   Params prm;
   prm.shader = cfg->shader;
   prm.spp = cfg->spp;
-  prm.max_depth = cfg->shader == CKR_SHADER_PATH ? std::max(1u, cfg->max_depth) : 1u;
+  const bool path = cfg->shader == CKR_SHADER_PATH || cfg->shader == CKR_SHADER_PATH_NEE;
+  if (cfg->shader == CKR_SHADER_PATH_NEE && s->n_emit == 0) return CKR_ERR_INVALID_ARGUMENT;
+  prm.max_depth = path ? std::max(1u, cfg->max_depth) : 1u;
   prm.n_light = cfg->n_light_samples;
-  prm.n_brdf = cfg->shader == CKR_SHADER_PATH ? 1u : cfg->n_brdf_samples;
-  prm.rr_prob = cfg->shader == CKR_SHADER_PATH ? cfg->rr_prob : 0.f;
+  prm.n_brdf = path ? 1u : cfg->n_brdf_samples;
+  prm.rr_prob = path ? cfg->rr_prob : 0.f;
   prm.seed = cfg->seed;
   prm.npix = cam->width * cam->height;
   uint32_t area_lights = 0, point_lights = 0;
   for (const DevLight &L : s->host_lights) (L.type == CKR_LIGHT_POINT ? point_lights : area_lights)++;
-  uint64_t per_path = (uint64_t)point_lights + (uint64_t)area_lights * prm.n_light +
-                      (cfg->shader == CKR_SHADER_DIRECT_MIS ? prm.n_brdf : 0);
+  uint64_t per_path = cfg->shader == CKR_SHADER_PATH_NEE
+                          ? 1u
+                          : (uint64_t)point_lights + (uint64_t)area_lights * prm.n_light +
+                                (cfg->shader == CKR_SHADER_DIRECT_MIS ? prm.n_brdf : 0);
   if (per_path > kNoAllocShadow) return CKR_ERR_TOO_LARGE;
   prm.shadow_per_path = (uint32_t)std::max<uint64_t>(1, per_path);
   uint64_t total = (uint64_t)prm.npix * prm.spp;
@@ -649,7 +921,7 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
     p += a256(bytes);
     return r;
   };
-  Paths P;
+  Paths P{};
   P.ray_o = reinterpret_cast<float4 *>(take(16ull * kNoAllocWave));
   P.ray_d = reinterpret_cast<float4 *>(take(16ull * kNoAllocWave));
   P.beta = reinterpret_cast<float4 *>(take(16ull * kNoAllocWave));
@@ -687,7 +959,8 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
   }
   const int g_ext = grid_for((const void *)k_extend, smem, kRTPB);
   const int g_sh = grid_for((const void *)k_shadow, smem, kRTPB);
-  const void *shade_fn = cfg->shader == CKR_SHADER_PATH ? (const void *)k_shade<CKR_SHADER_PATH>
+  const void *shade_fn = cfg->shader == CKR_SHADER_PATH_NEE ? (const void *)k_shade_nee
+                         : cfg->shader == CKR_SHADER_PATH      ? (const void *)k_shade<CKR_SHADER_PATH>
                          : cfg->shader == CKR_SHADER_DIRECT_MIS ? (const void *)k_shade<CKR_SHADER_DIRECT_MIS>
                                                                 : (const void *)k_shade<CKR_SHADER_DIRECT_MISCV>;
   const int g_shade = grid_for(shade_fn, 0, kRTPB);
@@ -699,15 +972,17 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
       k_extend<<<g_ext, kRTPB, smem, stream>>>(sv, P, cur, depth);
       CKR_CUDA_TRY(cudaMemsetAsync(P.counts + (cur ^ 1), 0, sizeof(uint32_t), stream));
       CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), stream));
-      if (cfg->shader == CKR_SHADER_PATH)
+      if (cfg->shader == CKR_SHADER_PATH_NEE)
+        k_shade_nee<<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, Learn{});
+      else if (cfg->shader == CKR_SHADER_PATH)
         k_shade<CKR_SHADER_PATH><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else if (cfg->shader == CKR_SHADER_DIRECT_MIS)
         k_shade<CKR_SHADER_DIRECT_MIS><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else
         k_shade<CKR_SHADER_DIRECT_MISCV><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
-      k_shadow<<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur);
+      k_shadow<<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur, nullptr);
       cur ^= 1;
-      if (cfg->shader != CKR_SHADER_PATH) break;
+      if (!path) break;
     }
   }
   uint32_t n3 = prm.npix * 3;

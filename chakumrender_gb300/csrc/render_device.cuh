@@ -2,6 +2,7 @@
 // surface interaction, light sampling and the MIS pdf sums of the reference's
 // MIS sampler (src/mis.cpp:18-223), offsets for secondary rays.
 #pragma once
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -185,6 +186,65 @@ __device__ __forceinline__ F3 sample_light(const ShadeView &sv, const DevLight &
   // The mesh sampler draws (index, sqrt(u1), u2); a tri light draws (sqrt(u0), u1).
   F3 p = L.type == CKR_LIGHT_MESH ? sample_triangle(A, B, C, e1, e2) : sample_triangle(A, B, C, e0, e1);
   return normalize(p - x);
+}
+
+// ---- one-sample NEE over many lights ---------------------------------------------
+// First index j of cdf[0, n) with cdf[j] > u (n >= 1; the last entry is 1).
+__device__ __forceinline__ uint32_t cdf_pick(const float *cdf, uint32_t n, float u) {
+  uint32_t lo = 0, hi = n - 1;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(cdf + mid) > u) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+__device__ __forceinline__ float cdf_mass(const float *cdf, uint32_t j) {
+  return __ldg(cdf + j) - (j ? __ldg(cdf + j - 1) : 0.f);
+}
+
+// Light-selection distribution at one vertex over the emitter lights
+// [first_emit, first_emit + n_emit): their power CDF, or the mixture
+// (1 - delta) p / sum(p) + delta / n_emit of a proposal's 64 probabilities p.
+struct Select {
+  const __half *p;  // nullptr: power
+  float scale, unif;
+};
+
+__device__ __forceinline__ Select make_select(const ShadeView &sv, const __half *p, float delta) {
+  Select s;
+  s.p = p;
+  s.scale = 0.f;
+  s.unif = 0.f;
+  if (p) {
+    float sum = 0.f;
+    for (uint32_t j = 0; j < sv.n_emit; ++j) sum += __half2float(p[j]);
+    s.scale = sum > 0.f ? (1.0f - delta) / sum : 0.f;
+    s.unif = (sum > 0.f ? delta : 1.0f) / (float)sv.n_emit;
+  }
+  return s;
+}
+
+__device__ __forceinline__ float select_prob(const ShadeView &sv, const Select &s, uint32_t j) {
+  return s.p ? s.scale * __half2float(s.p[j]) + s.unif : cdf_mass(sv.sel_cdf, j);
+}
+
+__device__ __forceinline__ uint32_t select_pick(const ShadeView &sv, const Select &s, float u) {
+  if (!s.p) return cdf_pick(sv.sel_cdf, sv.n_emit, u);
+  float run = 0.f;
+  for (uint32_t j = 0; j + 1 < sv.n_emit; ++j) {
+    run += s.scale * __half2float(s.p[j]) + s.unif;
+    if (u < run) return j;
+  }
+  return sv.n_emit - 1;
+}
+
+// Solid-angle pdf of the light technique for a direction that meets emitter
+// triangle `tri` of light k at distance t with |cos| cl at the emitter.
+__device__ __forceinline__ float nee_pdf(const ShadeView &sv, float q, const DevLight &L, uint32_t tri, float t,
+                                         float area, float cl) {
+  float ptri = cdf_mass(sv.pcdf + L.pcdf, tri - L.first);
+  return q * ptri * t * t / (area * cl);
 }
 
 }  // namespace ckr

@@ -21,7 +21,13 @@ struct DevLight {
   float px, py, pz;  // POINT: position; SPHERE: centre
   float radius;      // SPHERE
   float pr, pg, pb;  // POINT: power
+  uint32_t pcdf;     // MESH/TRI: offset of its per-triangle power CDF (one-sample NEE)
+  float power;       // MESH/TRI: emitted power sum of luminance(radiance) x area
+  float sel;         // MESH/TRI: power / total power of all MESH/TRI lights
+  float pad_;
 };
+
+constexpr uint32_t kNoLight = 0xFFFFFFFFu;
 
 constexpr uint32_t kInvCdfBins = 300;  // MeshLight::invCDFBins (headers/lightSources.h:150)
 
@@ -35,6 +41,11 @@ struct ShadeView {
   uint32_t nlights;
   uint32_t first_point;      // index of the first point light (= number of area/sphere lights)
   const uint32_t *cdf;       // mesh-light inverse CDFs (triangle offsets within the light)
+  // One-sample NEE over many lights (CKR_SHADER_PATH_NEE).
+  const uint32_t *tri_light;  // per triangle: its MESH/TRI light, or kNoLight
+  const float *pcdf;          // per-light triangle power CDFs (DevLight::pcdf)
+  const float *sel_cdf;       // power CDF over the emitter lights [first_emit, first_emit + n_emit)
+  uint32_t first_emit, n_emit;
 };
 
 }  // namespace ckr
@@ -54,7 +65,10 @@ struct ckr_scene {
   ckr::DevBuf<uint32_t> tri_mat, sph_mat, cdf;
   ckr::DevBuf<float> tri9;
   ckr::DevBuf<ckr::DevLight> lights;
-  uint32_t nlights = 0, first_point = 0;
+  ckr::DevBuf<uint32_t> tri_light;
+  ckr::DevBuf<float> pcdf, sel_cdf;
+  uint32_t nlights = 0, first_point = 0, first_emit = 0, n_emit = 0;
+  float bounds[6] = {0, 0, 0, 0, 0, 0};  // scene box (lo.xyz, hi.xyz) of triangles and spheres
   std::vector<ckr_material> host_mats;
   std::vector<ckr::DevLight> host_lights;
   // Renderer work buffers (path state, queues), grown on demand, owned here.

@@ -21,6 +21,11 @@ ShadeView shade_view_of(const ckr_scene *s) {
   v.nlights = s->nlights;
   v.first_point = s->first_point;
   v.cdf = s->cdf.ptr;
+  v.tri_light = s->tri_light.ptr;
+  v.pcdf = s->pcdf.ptr;
+  v.sel_cdf = s->sel_cdf.ptr;
+  v.first_emit = s->first_emit;
+  v.n_emit = s->n_emit;
   return v;
 }
 
@@ -110,6 +115,44 @@ extern "C" int ckr_scene_create_ex(const ckr_scene_desc *d, ckr_scene **out) {
                    [&](const DevLight &a, const DevLight &b) { return rank(a.type) < rank(b.type); });
   uint32_t first_point = 0;
   while (first_point < lights.size() && lights[first_point].type != CKR_LIGHT_POINT) ++first_point;
+  // One-sample NEE tables: each emitter triangle's light, per light the CDF of
+  // its triangles' power (luminance x area), and the power CDF over the
+  // MESH/TRI lights, which sit contiguously after the sphere lights.
+  uint32_t first_emit = 0;
+  while (first_emit < first_point && lights[first_emit].type == CKR_LIGHT_SPHERE) ++first_emit;
+  const uint32_t n_emit = first_point - first_emit;
+  std::vector<uint32_t> tri_light(d->ntri, kNoLight);
+  std::vector<float> pcdf, sel_cdf(n_emit);
+  double total = 0;
+  for (uint32_t k = first_emit; k < first_point; ++k) {
+    DevLight &g = lights[k];
+    g.pcdf = (uint32_t)pcdf.size();
+    std::vector<double> pw(g.count);
+    double sum = 0;
+    for (uint32_t i = 0; i < g.count; ++i) {
+      uint32_t tri = g.first + i;
+      uint32_t mi = d->tri_material ? d->tri_material[tri] : 0;
+      const float *r = d->materials[mi].radiance;
+      pw[i] = ((double)r[0] + r[1] + r[2]) / 3.0 * tri_area(d->tri9 + 9 * (size_t)tri);
+      sum += pw[i];
+      if (tri_light[tri] == kNoLight) tri_light[tri] = k;
+    }
+    double run = 0;
+    for (uint32_t i = 0; i < g.count; ++i) {
+      run += pw[i];
+      pcdf.push_back(sum > 0 ? (float)(run / sum) : (float)(i + 1) / (float)g.count);
+    }
+    if (g.count) pcdf.back() = 1.0f;
+    g.power = (float)sum;
+    total += sum;
+  }
+  double run = 0;
+  for (uint32_t k = first_emit; k < first_point; ++k) {
+    lights[k].sel = total > 0 ? (float)(lights[k].power / total) : 1.0f / (float)n_emit;
+    run += lights[k].power;
+    sel_cdf[k - first_emit] = total > 0 ? (float)(run / total) : (float)(k - first_emit + 1) / (float)n_emit;
+  }
+  if (n_emit) sel_cdf.back() = 1.0f;
   ckr_scene *s = nullptr;
   int st = ckr_scene_create(d->tri9, d->ntri, d->sph4, d->nsph, &d->build, &s);
   if (st != CKR_OK) return st;
@@ -120,12 +163,32 @@ extern "C" int ckr_scene_create_ex(const ckr_scene_desc *d, ckr_scene **out) {
       (st = upload(s->sph_mat, sm.data(), sm.size())) != CKR_OK ||
       (st = upload(s->tri9, d->tri9, 9 * (size_t)d->ntri)) != CKR_OK ||
       (st = upload(s->lights, lights.data(), lights.size())) != CKR_OK ||
-      (st = upload(s->cdf, cdf.data(), cdf.size())) != CKR_OK) {
+      (st = upload(s->cdf, cdf.data(), cdf.size())) != CKR_OK ||
+      (st = upload(s->tri_light, tri_light.data(), tri_light.size())) != CKR_OK ||
+      (st = upload(s->pcdf, pcdf.data(), pcdf.size())) != CKR_OK ||
+      (st = upload(s->sel_cdf, sel_cdf.data(), sel_cdf.size())) != CKR_OK) {
     ckr_scene_destroy(s);
     return st;
   }
   s->nlights = d->nlights;
   s->first_point = first_point;
+  s->first_emit = first_emit;
+  s->n_emit = n_emit;
+  float lo[3] = {3e38f, 3e38f, 3e38f}, hi[3] = {-3e38f, -3e38f, -3e38f};
+  for (size_t i = 0; i < 3 * (size_t)d->ntri; ++i)
+    for (int c = 0; c < 3; ++c) {
+      lo[c] = std::min(lo[c], d->tri9[3 * i + c]);
+      hi[c] = std::max(hi[c], d->tri9[3 * i + c]);
+    }
+  for (uint32_t i = 0; i < d->nsph; ++i)
+    for (int c = 0; c < 3; ++c) {
+      lo[c] = std::min(lo[c], d->sph4[4 * i + c] - d->sph4[4 * i + 3]);
+      hi[c] = std::max(hi[c], d->sph4[4 * i + c] + d->sph4[4 * i + 3]);
+    }
+  for (int c = 0; c < 3; ++c) {
+    s->bounds[c] = lo[c] <= hi[c] ? lo[c] : 0.f;
+    s->bounds[3 + c] = lo[c] <= hi[c] ? hi[c] : 0.f;
+  }
   s->host_mats.assign(d->materials, d->materials + nm);
   s->host_lights = lights;
   s->has_shading = true;

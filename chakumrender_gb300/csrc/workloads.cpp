@@ -257,3 +257,149 @@ extern "C" int ckr_workload_quad_lights(uint64_t seed, uint32_t nquads, float si
   }
   return CKR_OK;
 }
+
+// Many-light scene: the displaced icosphere (GGX, per-triangle roughness) in a
+// diffuse room whose ceiling and walls carry small emissive triangles, grouped
+// by k-means on their centroids into mesh lights (one light per cluster).
+extern "C" int ckr_workload_manylight(const ckr_manylight_spec *sp, float *tri9, uint32_t *tri_mat,
+                                      ckr_material *mats, ckr_light *lights, ckr_camera *cam, uint32_t *counts) {
+  if (!sp || !counts || sp->nemit == 0 || sp->nclusters == 0 || sp->nclusters > sp->nemit || sp->subdiv > 10)
+    return CKR_ERR_INVALID_ARGUMENT;
+  const uint32_t nmesh = 20u << (2 * sp->subdiv), nroom = 12, ne = sp->nemit;
+  const uint64_t ntri = (uint64_t)nmesh + nroom + ne;
+  if (ntri > 0xFFFFFFF0ull) return CKR_ERR_TOO_LARGE;
+  // Emitters: face, centre, orientation and radiance from the stream (seed, i).
+  const double lo = -5.0, hi = 5.0, y0 = sp->floor_y, y1 = sp->floor_y + 10.0, eps = 1e-3;
+  std::vector<D3> cen(ne);
+  std::vector<double> tri(9 * (size_t)ne), rad(ne);
+  for (uint32_t i = 0; i < ne; ++i) {
+    uint64_t key = ckr_key(sp->emit_seed, i);
+    uint32_t face = (uint32_t)(5.0 * ckr_draw_f(key, 0));
+    double u = 0.2 + 9.6 * ckr_draw_f(key, 1), v = 0.2 + 9.6 * ckr_draw_f(key, 2);
+    double th = 6.283185307179586 * ckr_draw_f(key, 3);
+    rad[i] = sp->radiance_lo * std::exp(std::log((double)sp->radiance_hi / sp->radiance_lo) * ckr_draw_f(key, 4));
+    D3 c, t, b;  // centre on the face, two in-plane axes
+    switch (face) {
+      case 0: c = d3(lo + u, y1 - eps, lo + v); t = d3(1, 0, 0); b = d3(0, 0, 1); break;   // ceiling
+      case 1: c = d3(lo + eps, y0 + u, lo + v); t = d3(0, 1, 0); b = d3(0, 0, 1); break;   // x = -5
+      case 2: c = d3(hi - eps, y0 + u, lo + v); t = d3(0, 1, 0); b = d3(0, 0, 1); break;   // x = +5
+      case 3: c = d3(lo + u, y0 + v, lo + eps); t = d3(1, 0, 0); b = d3(0, 1, 0); break;   // z = -5
+      default: c = d3(lo + u, y0 + v, hi - eps); t = d3(1, 0, 0); b = d3(0, 1, 0); break;  // z = +5
+    }
+    cen[i] = c;
+    const double r = sp->emit_side / std::sqrt(3.0);
+    for (int j = 0; j < 3; ++j) {
+      double a = th + 2.0943951023931957 * j;
+      D3 p = add(c, add(mul(t, r * std::cos(a)), mul(b, r * std::sin(a))));
+      tri[9 * i + 3 * j] = p.x;
+      tri[9 * i + 3 * j + 1] = p.y;
+      tri[9 * i + 3 * j + 2] = p.z;
+    }
+  }
+  // k-means (Lloyd), deterministic: centroids start at evenly spaced emitters.
+  const uint32_t K = sp->nclusters;
+  std::vector<D3> ctr(K);
+  for (uint32_t k = 0; k < K; ++k) ctr[k] = cen[(size_t)k * ne / K];
+  std::vector<uint32_t> asg(ne, 0);
+  for (int it = 0; it < 20; ++it) {
+    for (uint32_t i = 0; i < ne; ++i) {
+      double best = 1e300;
+      for (uint32_t k = 0; k < K; ++k) {
+        D3 d = sub(cen[i], ctr[k]);
+        double q = dot(d, d);
+        if (q < best) best = q, asg[i] = k;
+      }
+    }
+    std::vector<D3> sum(K, d3(0, 0, 0));
+    std::vector<uint32_t> cnt(K, 0);
+    for (uint32_t i = 0; i < ne; ++i) sum[asg[i]] = add(sum[asg[i]], cen[i]), ++cnt[asg[i]];
+    for (uint32_t k = 0; k < K; ++k)
+      if (cnt[k]) ctr[k] = mul(sum[k], 1.0 / cnt[k]);
+  }
+  std::vector<uint32_t> order(ne), start(K + 1, 0);
+  for (uint32_t i = 0; i < ne; ++i) ++start[asg[i] + 1];
+  for (uint32_t k = 0; k < K; ++k) start[k + 1] += start[k];
+  {
+    std::vector<uint32_t> fill(start.begin(), start.end() - 1);
+    for (uint32_t i = 0; i < ne; ++i) order[fill[asg[i]]++] = i;
+  }
+  uint32_t nl = 0;
+  for (uint32_t k = 0; k < K; ++k) nl += start[k + 1] > start[k];
+  counts[0] = (uint32_t)ntri;
+  counts[1] = nmesh + 1 + ne;  // materials
+  counts[2] = nl;
+  if (!tri9) return CKR_OK;  // size query
+  if (!tri_mat || !mats || !lights || !cam) return CKR_ERR_INVALID_ARGUMENT;
+  uint32_t n = 0;
+  int st = ckr_workload_icosphere(sp->subdiv, sp->noise_amp, sp->octaves, sp->mesh_seed, tri9, nmesh, &n);
+  if (st != CKR_OK) return st;
+  ckr_material m;
+  std::memset(&m, 0, sizeof(m));
+  for (uint32_t i = 0; i < nmesh; ++i) {
+    m.brdf = 2;  // GGX
+    m.alpha = (float)(sp->alpha_lo + ((double)sp->alpha_hi - sp->alpha_lo) * ckr_draw_f(ckr_key(sp->rough_seed, i), 0));
+    m.spec = sp->mesh_spec;
+    m.int_ior = 1e5f;  // F = 1 to within 4e-5
+    m.ext_ior = 1.0f;
+    m.reflectance = 1.0f;
+    m.color[0] = m.color[1] = m.color[2] = sp->mesh_albedo;
+    mats[i] = m;
+    tri_mat[i] = i;
+  }
+  // Room: 6 faces x 2 triangles, Lambertian (GGX with specularCoef 0).
+  std::memset(&m, 0, sizeof(m));
+  m.brdf = 2;
+  m.alpha = 0.5f;
+  m.int_ior = 1.5f;
+  m.ext_ior = 1.0f;
+  m.reflectance = 1.0f;
+  m.color[0] = m.color[1] = m.color[2] = sp->room_albedo;
+  mats[nmesh] = m;
+  const double P[8][3] = {{lo, y0, lo}, {hi, y0, lo}, {hi, y0, hi}, {lo, y0, hi},
+                          {lo, y1, lo}, {hi, y1, lo}, {hi, y1, hi}, {lo, y1, hi}};
+  const int Q[6][4] = {{0, 1, 2, 3}, {4, 7, 6, 5}, {0, 3, 7, 4}, {1, 5, 6, 2}, {0, 4, 5, 1}, {3, 2, 6, 7}};
+  for (int f = 0; f < 6; ++f) {
+    const int T[2][3] = {{Q[f][0], Q[f][1], Q[f][2]}, {Q[f][0], Q[f][2], Q[f][3]}};
+    for (int h = 0; h < 2; ++h) {
+      uint32_t id = nmesh + 2 * f + h;
+      for (int v = 0; v < 3; ++v)
+        for (int j = 0; j < 3; ++j) tri9[9 * (size_t)id + 3 * v + j] = (float)P[T[h][v]][j];
+      tri_mat[id] = nmesh;
+    }
+  }
+  // Emitters in cluster order, one material (radiance) each, one mesh light per cluster.
+  const uint32_t ebase = nmesh + nroom;
+  std::memset(&m, 0, sizeof(m));
+  m.light_type = 4;  // MESH
+  for (uint32_t s = 0; s < ne; ++s) {
+    uint32_t i = order[s];
+    for (int j = 0; j < 9; ++j) tri9[9 * (size_t)(ebase + s) + j] = (float)tri[9 * (size_t)i + j];
+    m.radiance[0] = m.radiance[1] = m.radiance[2] = (float)rad[i];
+    mats[nmesh + 1 + s] = m;
+    tri_mat[ebase + s] = nmesh + 1 + s;
+  }
+  uint32_t l = 0;
+  for (uint32_t k = 0; k < K; ++k) {
+    if (start[k + 1] == start[k]) continue;
+    ckr_light L;
+    std::memset(&L, 0, sizeof(L));
+    L.type = CKR_LIGHT_MESH;
+    L.first = ebase + start[k];
+    L.count = start[k + 1] - start[k];
+    lights[l++] = L;
+  }
+  // Camera in the reference's convention (src/prepareScene.cpp:12-36).
+  D3 pos = d3(sp->cam_pos[0], sp->cam_pos[1], sp->cam_pos[2]);
+  D3 cd = normalize(sub(d3(sp->cam_target[0], sp->cam_target[1], sp->cam_target[2]), pos));
+  D3 cx = normalize(cross(cd, d3(0, 1, 0)));
+  const double tf = std::tan(sp->fov_deg * 3.141592653589793 / 360.0);
+  cx = mul(cx, (double)sp->width / sp->height * tf);
+  D3 cy = mul(normalize(cross(cx, cd)), tf);
+  std::memset(cam, 0, sizeof(*cam));
+  const D3 src[4] = {pos, cd, cx, cy};
+  float *dst[4] = {cam->pos, cam->dir, cam->cx, cam->cy};
+  for (int k = 0; k < 4; ++k) dst[k][0] = (float)src[k].x, dst[k][1] = (float)src[k].y, dst[k][2] = (float)src[k].z;
+  cam->width = sp->width;
+  cam->height = sp->height;
+  return CKR_OK;
+}

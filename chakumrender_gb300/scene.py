@@ -15,6 +15,7 @@ F3 = C.c_float * 3
 SHADER_DIRECT_MISCV = 0
 SHADER_DIRECT_MIS = 1
 SHADER_PATH = 2
+SHADER_PATH_NEE = 3
 LIGHT_MESH, LIGHT_TRI, LIGHT_SPHERE, LIGHT_POINT = 0, 1, 2, 3
 SCENES = Path(__file__).resolve().parent / "scenes"
 
@@ -77,10 +78,16 @@ class SceneData:
         self.tri_mat = np.ascontiguousarray(tri_mat, np.uint32)
         self.sph4 = np.ascontiguousarray(sph4, np.float32).reshape(-1, 4)
         self.sph_mat = np.ascontiguousarray(sph_mat, np.uint32)
-        self.materials = (Material * max(1, len(materials)))(*materials)
-        self.nmat = len(materials)
-        self.lights = (Light * max(1, len(lights)))(*lights)
-        self.nlights = len(lights)
+        if isinstance(materials, C.Array):  # already a ctypes array (large scenes)
+            self.materials, self.nmat = materials, len(materials)
+        else:
+            self.materials = (Material * max(1, len(materials)))(*materials)
+            self.nmat = len(materials)
+        if isinstance(lights, C.Array):
+            self.lights, self.nlights = lights, len(lights)
+        else:
+            self.lights = (Light * max(1, len(lights)))(*lights)
+            self.nlights = len(lights)
         self.camera = camera
 
     def desc(self, max_leaf: int = 0) -> SceneDesc:
@@ -143,3 +150,47 @@ def write_ppm(path, rgb: np.ndarray) -> None:
     rgb = np.ascontiguousarray(rgb, np.float32)
     h, w = rgb.shape[:2]
     check(_setup().ckr_write_ppm(str(path).encode(), _ptr(rgb), w, h), "ckr_write_ppm")
+
+
+class ManylightSpec(C.Structure):
+    _fields_ = [("subdiv", U32), ("octaves", U32), ("noise_amp", C.c_float), ("mesh_seed", C.c_uint64),
+                ("rough_seed", C.c_uint64), ("emit_seed", C.c_uint64), ("alpha_lo", C.c_float),
+                ("alpha_hi", C.c_float), ("mesh_spec", C.c_float), ("mesh_albedo", C.c_float),
+                ("room_albedo", C.c_float), ("floor_y", C.c_float), ("nemit", U32), ("nclusters", U32),
+                ("emit_side", C.c_float), ("radiance_lo", C.c_float), ("radiance_hi", C.c_float),
+                ("cam_pos", F3), ("cam_target", F3), ("fov_deg", C.c_float), ("width", U32), ("height", U32)]
+
+
+def manylight_spec(subdiv=8, nemit=4096, nclusters=64, width=1920, height=1080, **kw) -> ManylightSpec:
+    """The many-light scene: the 1,310,720-triangle displaced icosphere (GGX, roughness
+    uniform per triangle in [0.1, 0.8], seed 3) in a 10^3 diffuse room with 4,096
+    emissive triangles on its ceiling and walls (radiance log-uniform in [0.5, 50])
+    grouped into 64 clusters."""
+    s = ManylightSpec(subdiv=subdiv, octaves=6, noise_amp=0.05, mesh_seed=1, rough_seed=3, emit_seed=5,
+                      alpha_lo=0.1, alpha_hi=0.8, mesh_spec=1.0, mesh_albedo=0.9, room_albedo=0.7, floor_y=-1.2,
+                      nemit=nemit, nclusters=nclusters, emit_side=0.12, radiance_lo=0.5, radiance_hi=50.0,
+                      cam_pos=F3(0.0, 0.6, 3.4), cam_target=F3(0.0, 0.0, 0.0), fov_deg=45.0, width=width,
+                      height=height)
+    for k, v in kw.items():
+        setattr(s, k, F3(*v) if k in ("cam_pos", "cam_target") else v)
+    return s
+
+
+def manylight_scene(spec: ManylightSpec | None = None) -> SceneData:
+    L = lib()
+    if not getattr(L, "_ml_sig", False):
+        L.ckr_workload_manylight.argtypes = [P, P, P, P, P, P, P]
+        L.ckr_workload_manylight.restype = C.c_int
+        L._ml_sig = True
+    spec = spec or manylight_spec()
+    counts = (U32 * 3)()
+    check(L.ckr_workload_manylight(C.byref(spec), None, None, None, None, None, counts), "manylight size")
+    ntri, nmat, nl = counts
+    tri = np.empty((ntri, 9), np.float32)
+    tri_mat = np.empty(ntri, np.uint32)
+    mats = (Material * nmat)()
+    lights = (Light * nl)()
+    cam = Camera()
+    check(L.ckr_workload_manylight(C.byref(spec), _ptr(tri), _ptr(tri_mat), C.addressof(mats), C.addressof(lights),
+                                   C.byref(cam), counts), "manylight")
+    return SceneData(tri, tri_mat, np.zeros((0, 4), np.float32), np.zeros(0, np.uint32), mats, lights, cam)

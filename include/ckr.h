@@ -189,6 +189,15 @@ typedef struct ckr_camera {
 #define CKR_SHADER_DIRECT_MISCV 0 /* shadeDirectOnly + getLightFromMeshSource_Analytic_MISCV (reference default) */
 #define CKR_SHADER_DIRECT_MIS 1   /* shadeDirectOnly + getLightFromAllSources_MIS */
 #define CKR_SHADER_PATH 2         /* path tracer: MIS light/BRDF at every vertex, BRDF-sampled continuation */
+/* Many-light path tracer (no reference counterpart: the reference's
+ * getLightFromAllSources_MIS samples every light, src/mis.cpp:100-146): at every
+ * vertex ONE light sample -- an emitter light (MESH/TRI; "cluster") drawn from the
+ * selection distribution, one of its triangles in proportion to power
+ * (luminance x area), a uniform point on it -- and one BRDF sample
+ * (getBrdfDirectionSampleRandomized) that also continues the path; balance
+ * heuristic between the two; Russian roulette with rr_prob.  ckr_render selects
+ * lights in proportion to power; ckr_render_learned with a proposal network. */
+#define CKR_SHADER_PATH_NEE 3
 
 typedef struct ckr_render_cfg {
   uint32_t shader;           /* CKR_SHADER_* */
@@ -226,6 +235,56 @@ int ckr_render(ckr_scene *scene, const ckr_camera *cam, const ckr_render_cfg *cf
  * the GPU (other streams or host threads) race: serialise them. */
 int ckr_render_noalloc(ckr_scene *scene, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb,
                        void *stream);
+
+/* ---- learned light selection (no reference counterpart) -------------------
+ * A proposal is a small network that maps a shading point (position, normal,
+ * outgoing direction, GGX roughness) to a distribution over the scene's emitter
+ * lights ("clusters", at most 64): 96 inputs (12-frequency sin/cos encoding of
+ * the position normalised to the scene box, n, wo, alpha, 1), three hidden
+ * layers of 64 with ReLU, softmax.  BF16 weights and activations, FP32
+ * accumulation, evaluated and trained on the tensor cores.  The renderer draws
+ * lights from (1 - defensive) * network + defensive * uniform and weights the
+ * light sample against the BRDF sample by the balance heuristic, so estimates
+ * stay unbiased whatever the network says.  Training is online: every bounce's
+ * light samples (position, cluster, luminance of the unoccluded contribution /
+ * pdf) feed one Adam step minimising the cross-entropy between the clusters'
+ * contributions and the network's distribution. */
+typedef struct ckr_proposal ckr_proposal;
+typedef struct ckr_proposal_cfg {
+  uint64_t seed;      /* weight initialisation stream */
+  float lr;           /* Adam learning rate (1e-3) */
+  float defensive;    /* uniform fraction of the selection mixture, (0, 1] (0.2) */
+  uint32_t batch;     /* training records kept per bounce (65536) */
+  uint32_t train;     /* 1: train while rendering */
+  uint32_t minibatch; /* records per Adam step, batch / minibatch steps per bounce (16384; 0: batch) */
+  uint32_t reserved;
+} ckr_proposal_cfg;
+#define CKR_PROPOSAL_NPARAMS 18624 /* W1[64][96], W2[64][64], b2, W3, b3, W4, b4 */
+
+/* cfg NULL: the defaults above.  CKR_ERR_TOO_LARGE if the scene has more than 64
+ * MESH/TRI lights, CKR_ERR_INVALID_ARGUMENT if it has none. */
+int ckr_proposal_create(const ckr_scene *scene, const ckr_proposal_cfg *cfg, ckr_proposal **out);
+int ckr_proposal_destroy(ckr_proposal *p);
+int ckr_proposal_set_training(ckr_proposal *p, int train);
+/* FP32 master weights (host buffers of CKR_PROPOSAL_NPARAMS floats); setting
+ * them resets the optimiser state. */
+int ckr_proposal_get_params(ckr_proposal *p, float *params);
+int ckr_proposal_set_params(ckr_proposal *p, const float *params);
+/* The position normalisation (p - centre) * scale and the number of clusters. */
+int ckr_proposal_encoding(const ckr_proposal *p, float centre[3], float *scale, uint32_t *nclusters);
+/* Direct use on caller records (device, 16-byte aligned, 12 floats each:
+ * x.xyz, alpha, n.xyz, weight, wo.xyz, cluster index as uint32 bits): network
+ * probabilities (FP16 bits, 64 per record), or one training step. */
+int ckr_proposal_infer(ckr_proposal *p, const float *rec12, uint32_t n, uint16_t *probs, void *stream);
+int ckr_proposal_train_step(ckr_proposal *p, const float *rec12, uint32_t n, void *stream);
+/* Synchronises; Adam steps taken and the last step's loss.  Returns a device
+ * error recorded by the network kernels (CKR_ERR_ITERATION_LIMIT), then clears it. */
+int ckr_proposal_status(ckr_proposal *p, uint32_t *steps, float *last_loss);
+
+/* ckr_render with cfg->shader = CKR_SHADER_PATH_NEE and lights drawn from the
+ * proposal (trained online while rendering if its training flag is set). */
+int ckr_render_learned(ckr_scene *scene, ckr_proposal *proposal, const ckr_camera *cam, const ckr_render_cfg *cfg,
+                       float *rgb, double *accum, void *stream);
 
 /* Rays traced by ckr_render on this scene since the last reset: closest-hit
  * rays (camera + continuation) and shadow rays.  Synchronises the device. */
@@ -317,6 +376,30 @@ int ckr_workload_rays_pinhole(const float eye[3], const float target[3], const f
  * ray i is a function of (seed, i) only. */
 int ckr_workload_rays_incoherent(const float lo[3], const float hi[3], uint64_t seed,
                                  uint32_t n, float tmax_lo, float tmax_hi, ckr_ray *out);
+
+/* Many-light scene: the displaced icosphere of ckr_workload_icosphere
+ * (GGX, F = 1, specularCoef mesh_spec, roughness uniform in [alpha_lo, alpha_hi]
+ * per triangle from stream rough_seed) inside the room [-5,5] x
+ * [floor_y, floor_y + 10] x [-5,5] (Lambertian, albedo room_albedo).  nemit
+ * equilateral emitters of side emit_side lie 1e-3 inside the ceiling and the four
+ * walls (face, position, rotation from stream (emit_seed, i)), radiance
+ * log-uniform in [radiance_lo, radiance_hi], grouped by 20 Lloyd iterations of
+ * k-means on their centroids into nclusters mesh lights.  Triangle order: mesh,
+ * room (12), emitters by cluster.  Materials: one per mesh triangle, the room,
+ * one per emitter.  counts receives (ntri, nmaterials, nlights); with tri9 NULL
+ * only counts is written (size query). */
+typedef struct ckr_manylight_spec {
+  uint32_t subdiv, octaves;
+  float noise_amp;
+  uint64_t mesh_seed, rough_seed, emit_seed;
+  float alpha_lo, alpha_hi, mesh_spec, mesh_albedo, room_albedo, floor_y;
+  uint32_t nemit, nclusters;
+  float emit_side, radiance_lo, radiance_hi;
+  float cam_pos[3], cam_target[3], fov_deg;
+  uint32_t width, height;
+} ckr_manylight_spec;
+int ckr_workload_manylight(const ckr_manylight_spec *spec, float *tri9, uint32_t *tri_material,
+                           ckr_material *materials, ckr_light *lights, ckr_camera *cam, uint32_t counts[3]);
 
 /* The library's counter-based stream (see csrc/ckr_rng.h), for checkers. */
 float ckr_rng_uniform(uint64_t seed, uint64_t index, uint32_t counter);

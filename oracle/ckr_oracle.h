@@ -114,6 +114,26 @@ struct ckr_render_cfg;
 void orc_render(const struct ckr_scene_desc *desc, const struct ckr_camera *cam, const struct ckr_render_cfg *cfg,
                 double *rgb, int threads);
 
+/* ---------------------------------------------------------------------- */
+/* Learned light-selection network (orc_mlp.c; no reference counterpart).  */
+/* ---------------------------------------------------------------------- */
+#define ORC_MLP_IN 96
+#define ORC_MLP_HIDDEN 64
+#define ORC_MLP_OUT 64
+#define ORC_MLP_FREQS 12
+#define ORC_MLP_NPARAMS (64 * 96 + 3 * (64 * 64 + 64))
+/* The 96 input features of one 12-float record. */
+void orc_mlp_features(const float *rec12, const double *centre, double scale, double *f96);
+/* probs: n x 64, softmax over the first nclusters outputs (the rest 0). */
+void orc_mlp_forward(const double *params, const float *rec12, uint32_t n, const double *centre, double scale,
+                     uint32_t nclusters, double *probs);
+/* Loss and its gradient over n records; returns 0 (and zeros) when the weights sum to 0. */
+int orc_mlp_loss_grad(const double *params, const float *rec12, uint32_t n, const double *centre, double scale,
+                      uint32_t nclusters, double *grad, double *loss);
+/* One Adam step (step = 1, 2, ...). */
+void orc_mlp_adam(double *params, double *m, double *v, const double *grad, uint32_t n, uint32_t step, double lr,
+                  double beta1, double beta2, double eps);
+
 /* One direction sample from uniforms (e1, e2); see orc_shading.c for `kind`. */
 void orc_sample_dir(int kind, const double *n3, const double *w3, double param, double e1, double e2, double *out3);
 

@@ -52,6 +52,10 @@ def orc() -> C.CDLL:
         _sig(L, "orc_ltc_shade_batch", [P, U32, P, P, P, P, P, U32, P, C.c_int], None)
         _sig(L, "orc_sample_dir", [C.c_int, P, P, C.c_double, C.c_double, C.c_double, P], None)
         _sig(L, "orc_ltc_mc", [P, U32, P, P, P, P, P, U32, U32, C.c_uint64, P, P, C.c_int], None)
+        _sig(L, "orc_mlp_forward", [P, P, U32, P, C.c_double, U32, P], None)
+        _sig(L, "orc_mlp_loss_grad", [P, P, U32, P, C.c_double, U32, P, P], C.c_int)
+        _sig(L, "orc_mlp_adam", [P, P, P, P, U32, U32, C.c_double, C.c_double, C.c_double, C.c_double], None)
+        _sig(L, "orc_mlp_features", [P, P, C.c_double, P], None)
         if L.orc_ltc_load(str(LTC_TABLE).encode()) != 0:
             raise RuntimeError(f"cannot load {LTC_TABLE}")
         _orc = L
@@ -216,6 +220,47 @@ def ltc_mc(mat, x, n, v, light_tri9, light_rgb, spp: int, seed: int, pixel_index
     orc().orc_ltc_mc(_p(mat), len(mat), _p(x), _p(n), _p(v), _p(lt), _p(lc), len(lt), spp, seed,
                      None if idx is None else _p(idx), _p(out), threads)
     return out
+
+
+MLP_NPARAMS = 64 * 96 + 3 * (64 * 64 + 64)
+
+
+def mlp_features(rec12, centre, scale) -> np.ndarray:
+    rec = np.ascontiguousarray(rec12, dtype=np.float32).reshape(-1, 12)
+    c = np.ascontiguousarray(centre, dtype=np.float64)
+    out = np.empty((len(rec), 96))
+    for i in range(len(rec)):
+        orc().orc_mlp_features(rec[i].ctypes.data, _p(c), scale, out[i].ctypes.data)
+    return out
+
+
+def mlp_forward(params, rec12, centre, scale, nclusters) -> np.ndarray:
+    """The light-selection network in FP64: n x 64 probabilities (see orc_mlp.c)."""
+    prm = np.ascontiguousarray(params, dtype=np.float64)
+    rec = np.ascontiguousarray(rec12, dtype=np.float32).reshape(-1, 12)
+    c = np.ascontiguousarray(centre, dtype=np.float64)
+    out = np.empty((len(rec), 64))
+    orc().orc_mlp_forward(_p(prm), _p(rec), len(rec), _p(c), scale, nclusters, _p(out))
+    return out
+
+
+def mlp_loss_grad(params, rec12, centre, scale, nclusters):
+    """(loss, gradient) of the training objective over the records; (0, zeros) if all weights are 0."""
+    prm = np.ascontiguousarray(params, dtype=np.float64)
+    rec = np.ascontiguousarray(rec12, dtype=np.float32).reshape(-1, 12)
+    c = np.ascontiguousarray(centre, dtype=np.float64)
+    g = np.empty(MLP_NPARAMS)
+    loss = C.c_double(0)
+    orc().orc_mlp_loss_grad(_p(prm), _p(rec), len(rec), _p(c), scale, nclusters, _p(g), C.byref(loss))
+    return loss.value, g
+
+
+def mlp_adam(params, m, v, grad, step, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+    """In place on float64 arrays params, m, v."""
+    for a in (params, m, v):
+        assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    g = np.ascontiguousarray(grad, dtype=np.float64)
+    orc().orc_mlp_adam(_p(params), _p(m), _p(v), _p(g), len(params), step, lr, beta1, beta2, eps)
 
 
 def sample_dir(kind: int, n, w, param: float, e1: float, e2: float) -> np.ndarray:

@@ -265,6 +265,89 @@ def bench_ltc(torch, steps: int):
                               "mc_ms": round(mc_ms, 2)}}
 
 
+def bench_manylight(torch):
+    """The many-light scene (1,310,720-triangle displaced icosphere, GGX roughness
+    uniform per triangle in [0.1, 0.8], 10^3 room, 4,096 emissive triangles in 64
+    clusters), 1920x1080, 64 spp, max depth 6, one-sample NEE path tracer.  Plain =
+    lights chosen in proportion to power; learned = the proposal network (BF16
+    tensor-core MLP, defensive 0.2, Adam 1e-3) trained online from scratch inside
+    the timed frame (cold) or carried over from one earlier frame (warm).  relMSE is
+    taken over a 320x180 window of the frame against a 16,384-spp FP64-accumulated
+    render of that window; the learned frame gets the spp that fit in the plain
+    frame's time."""
+    from chakumrender_gb300 import scene as S
+    from chakumrender_gb300.proposal import Proposal
+
+    W, H, SPP, DEPTH = 1920, 1080, 64, 6
+    X0, Y0, CW, CH = 800, 300, 320, 180  # window (x from the left, y from the bottom)
+    sd = S.manylight_scene(S.manylight_spec(width=W, height=H))
+    scene = S.RenderScene(sd)
+    cam = sd.camera
+    win = S.Camera()
+    cx, cy, d = np.array(cam.cx, float), np.array(cam.cy, float), np.array(cam.dir, float)
+    nd = d + cx * ((X0 + CW / 2) / W - .5) + cy * ((Y0 + CH / 2) / H - .5)
+    for k in range(3):
+        win.pos[k], win.dir[k], win.cx[k], win.cy[k] = cam.pos[k], nd[k], cx[k] * CW / W, cy[k] * CH / H
+    win.width, win.height = CW, CH
+    rgb = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+    wrgb = torch.empty((CH, CW, 3), dtype=torch.float32, device="cuda")
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t
+
+    cfg = lambda spp, seed: S.render_cfg(shader=S.SHADER_PATH_NEE, spp=spp, max_depth=DEPTH, seed=seed)
+    ref_sec = timed(lambda: scene.render(win, cfg(16384, 1000), wrgb.data_ptr()))
+    ref = wrgb.double().cpu().numpy()
+
+    def rel_mse():
+        img = rgb.double().cpu().numpy()[H - Y0 - CH:H - Y0, X0:X0 + CW]
+        return float(np.mean((img - ref) ** 2 / (ref * ref + 1e-2)))
+
+    scene.render(cam, cfg(SPP, 1), rgb.data_ptr())  # warm-up
+    scene.ray_stats(reset=True)
+    t_plain = timed(lambda: scene.render(cam, cfg(SPP, 2), rgb.data_ptr()))
+    closest, shadow = scene.ray_stats(reset=True)
+    e_plain = rel_mse()
+    opts = dict(minibatch=4096, max_steps=1000)
+    cold = Proposal(scene, seed=1, **opts)
+    t_cold64 = timed(lambda: cold.render(cam, cfg(SPP, 3), rgb.data_ptr()))
+    e_cold64 = rel_mse()
+    spp_cold = max(2, int(SPP * t_plain / t_cold64))
+    cold2 = Proposal(scene, seed=2, **opts)
+    t_cold = timed(lambda: cold2.render(cam, cfg(spp_cold, 4), rgb.data_ptr()))
+    e_cold = rel_mse()
+    cold.set_training(False)  # warm: the network of the first learned frame, frozen
+    t_warm64 = timed(lambda: cold.render(cam, cfg(SPP, 5), rgb.data_ptr()))
+    e_warm64 = rel_mse()
+    spp_warm = max(2, int(SPP * t_plain / t_warm64))
+    t_warm = timed(lambda: cold.render(cam, cfg(spp_warm, 6), rgb.data_ptr()))
+    e_warm = rel_mse()
+    st, steps, loss = cold2.status()
+    if st != 0:
+        raise RuntimeError(f"proposal network error {st}")
+    samples = W * H * SPP
+    return {"workload": "many-light: 1,310,720-tri GGX icosphere in a 10^3 room, 4,096 emitters in 64 clusters, "
+                        "1920x1080, 64 spp, depth 6, one-sample NEE",
+            "plain": {"spp": SPP, "sec": round(t_plain, 4), "relmse": round(e_plain, 5),
+                      "samples_per_s": round(samples / t_plain, 1),
+                      "mrays_per_s": round((closest + shadow) / t_plain / 1e6, 1)},
+            "learned_cold_64spp": {"sec": round(t_cold64, 4), "relmse": round(e_cold64, 5)},
+            "learned_cold_equal_time": {"spp": spp_cold, "sec": round(t_cold, 4), "relmse": round(e_cold, 5),
+                                        "adam_steps": steps, "last_loss": round(loss, 4)},
+            "learned_warm_64spp": {"sec": round(t_warm64, 4), "relmse": round(e_warm64, 5)},
+            "learned_warm_equal_time": {"spp": spp_warm, "sec": round(t_warm, 4), "relmse": round(e_warm, 5)},
+            "relmse_ratio_plain_over_learned_equal_time": {"cold": round(e_plain / e_cold, 3),
+                                                           "warm": round(e_plain / e_warm, 3)},
+            "reference": {"spp": 16384, "window": [X0, Y0, CW, CH], "sec": round(ref_sec, 2),
+                          "accumulation": "fp64"},
+            "proposal": {"minibatch": opts["minibatch"], "max_steps": opts["max_steps"], "defensive": 0.2,
+                         "lr": 1e-3}}
+
+
 def cpu_side_baselines(tri_unused=None):
     """FP64 restatements of the reference on the host cores for the box render
     (path tracer, 64x64 x 16 spp sample) and LTC shading (65,536 pixels)."""
@@ -427,6 +510,7 @@ def main():
     }
     line["box_render"] = bench_box_render(torch, args.steps)
     line["ltc_shade"] = bench_ltc(torch, args.steps)
+    line["manylight"] = bench_manylight(torch)
     if not args.no_cpu_baseline:
         cb, ref_counts = cpu_baseline(tri, closest)
         line["cpu_baseline"] = cb

@@ -2,11 +2,14 @@
 // cores: inference (k_mlp_infer), training forward + backward (k_mlp_train) and
 // the Adam update (k_mlp_adam), all for tiles of 128 rows.
 //
-// One CTA of 128 threads owns a tile: thread t computes row t's features and
+// A group of 128 threads owns a tile: thread t computes row t's features and
 // epilogues, thread 0 issues the tcgen05.mma chain of each layer (M = 128 rows,
-// N = 64 outputs, K = 96 or 64 in steps of 16) into tensor memory and commits it
-// to an mbarrier that the CTA waits on with a bounded poll.  Row t of the
-// accumulator lives in TMEM lane t, which warp t / 32 reads with tcgen05.ld.
+// N = 64 outputs, K = 96, or 80 for the hidden layers whose operands carry a
+// constant 1 that multiplies the bias) into tensor memory and commits it to an
+// mbarrier that the group waits on with a bounded poll.  Row t of the
+// accumulator lives in TMEM lane t, which warp (t / 32) % 4 reads with
+// tcgen05.ld.  Inference runs two groups per CTA over the same weights, so one
+// group's epilogue overlaps the other's MMAs; training runs one.
 //
 // Backward pass, per layer l with input activations X (rows b) and output
 // gradient G (rows b):  dW^T = X^T G  (M = input features padded to 128,
@@ -29,13 +32,13 @@
 #include "ckr_internal.h"
 #include "ckr_rng.h"
 #include "mlp.h"
+#include "render_device.cuh"
 #include "tc05.cuh"
 
 namespace ckr {
 namespace mlp {
 namespace {
 
-constexpr uint32_t kTPB = 128;
 constexpr uint32_t kWaitTries = 1u << 22;
 constexpr uint32_t kIdesc = tc::idesc_bf16(128, 64);
 
@@ -77,10 +80,23 @@ __device__ __forceinline__ void write_features(uint8_t *x0, uint32_t t, float4 r
                                                const Params &p) {
   float f[kIn];
   const float pc[3] = {(r0.x - p.cx) * p.scale, (r0.y - p.cy) * p.scale, (r0.z - p.cz) * p.scale};
+  // sin, cos of 2^k pi p: the base frequency, then the double-angle recurrences
+  // sin 2a = 2 sin a cos a, cos 2a = (cos a - sin a)(cos a + sin a); the error
+  // (about 1e-6 at the base) roughly doubles per octave, a few 1e-3 after eleven,
+  // at the level of BF16's rounding of the features.
 #pragma unroll
-  for (int c = 0; c < 3; ++c)
+  for (int c = 0; c < 3; ++c) {
+    float sn, cs;
+    __sincosf(3.14159265358979f * pc[c], &sn, &cs);  // |argument| <= pi inside the scene box
 #pragma unroll
-    for (int k = 0; k < (int)kFreqs; ++k) sincospif(ldexpf(pc[c], k), &f[24 * c + 2 * k], &f[24 * c + 2 * k + 1]);
+    for (int k = 0; k < (int)kFreqs; ++k) {
+      f[24 * c + 2 * k] = sn;
+      f[24 * c + 2 * k + 1] = cs;
+      const float s2 = 2.0f * sn * cs;
+      cs = (cs - sn) * (cs + sn);
+      sn = s2;
+    }
+  }
   f[72] = r1.x; f[73] = r1.y; f[74] = r1.z;
   f[75] = r2.x; f[76] = r2.y; f[77] = r2.z;
   f[78] = r0.w;
@@ -91,38 +107,63 @@ __device__ __forceinline__ void write_features(uint8_t *x0, uint32_t t, float4 r
   for (int q = 0; q < (int)kIn / 8; ++q) st8(x0, t, 8 * q, kIn, f + 8 * q);
 }
 
-// Accumulator row (64 columns) + bias, ReLU, into row t of a K = 64 operand.
-__device__ __forceinline__ void epilogue_relu(uint32_t taddr, const float *bias, uint8_t *dst, uint32_t t) {
+// Two FP32 values to a BF16 pair with ReLU (lower half = first value).
+__device__ __forceinline__ uint32_t pack_relu_bf16(float lo, float hi) {
+  uint32_t r;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+
+// Accumulator row t (64 columns, bias included by the MMA) through ReLU into row t
+// of a hidden-layer operand (K = 80): columns 0..63, then the constant 1 at 64 and
+// zeros to 79.
+__device__ __forceinline__ void epilogue_relu(uint32_t taddr, uint8_t *dst, uint32_t t) {
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     float v[32];
     tc::tmem_ld32(taddr + 32 * h, v);
 #pragma unroll
-    for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + (bias ? bias[32 * h + j] : 0.f), 0.f);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) st8(dst, t, 32 * h + 8 * q, 64, v + 8 * q);
+    for (int q = 0; q < 4; ++q) {
+      const float *x = v + 8 * q;
+      *reinterpret_cast<uint4 *>(dst + tc::kmaj(t, 32 * h + 8 * q, kHidK)) =
+          make_uint4(pack_relu_bf16(x[0], x[1]), pack_relu_bf16(x[2], x[3]), pack_relu_bf16(x[4], x[5]),
+                     pack_relu_bf16(x[6], x[7]));
+    }
   }
+  *reinterpret_cast<uint4 *>(dst + tc::kmaj(t, 64, kHidK)) = make_uint4(0x3F80u, 0u, 0u, 0u);  // BF16 1.0
+  *reinterpret_cast<uint4 *>(dst + tc::kmaj(t, 72, kHidK)) = make_uint4(0u, 0u, 0u, 0u);
 }
 
-// Softmax over the first C logits (accumulator + bias) of row t.
-__device__ __forceinline__ void softmax_row(uint32_t taddr, const float *bias, uint32_t C, float *p) {
+// exp(z) over the logits of row t when all 64 are clusters, with z clamped to
+// [-80, 80] so that neither the terms nor their sum leave FP32's range (the
+// softmax does not change for logits inside that range); returns the sum.
+__device__ __forceinline__ float softmax_exp64(uint32_t taddr, float *p) {
+  tc::tmem_ld32(taddr, p);
+  tc::tmem_ld32(taddr + 32, p + 32);
+  float sum = 0.f;
+#pragma unroll
+  for (int j = 0; j < 64; ++j) {
+    p[j] = __expf(fminf(fmaxf(p[j], -80.f), 80.f));
+    sum += p[j];
+  }
+  return sum;
+}
+
+// exp(z - max) over the first C logits of row t (0 beyond); returns their sum.
+__device__ __forceinline__ float softmax_exp(uint32_t taddr, uint32_t C, float *p) {
   tc::tmem_ld32(taddr, p);
   tc::tmem_ld32(taddr + 32, p + 32);
   float mx = -3.0e38f;
 #pragma unroll
-  for (int j = 0; j < 64; ++j) {
-    p[j] += bias[j];
+  for (int j = 0; j < 64; ++j)
     if ((uint32_t)j < C) mx = fmaxf(mx, p[j]);
-  }
   float sum = 0.f;
 #pragma unroll
   for (int j = 0; j < 64; ++j) {
     p[j] = (uint32_t)j < C ? __expf(p[j] - mx) : 0.f;
     sum += p[j];
   }
-  const float inv = 1.0f / sum;
-#pragma unroll
-  for (int j = 0; j < 64; ++j) p[j] *= inv;
+  return sum;
 }
 
 __device__ __forceinline__ void issue(uint32_t d, uint32_t a, uint32_t b, uint32_t K, uint32_t accumulate_first) {
@@ -130,20 +171,29 @@ __device__ __forceinline__ void issue(uint32_t d, uint32_t a, uint32_t b, uint32
     tc::mma_bf16(d, tc::sdesc(a, K, s), tc::sdesc(b, K, s), kIdesc, (s > 0 || accumulate_first) ? 1u : 0u);
 }
 
-// Every thread: shared-memory writes visible to the tensor core, TMEM reads done.
-__device__ __forceinline__ void sync_for_mma() {
-  tc::fence_proxy_async();
-  tc::fence_before_sync();
-  __syncthreads();
+// Barrier of one 128-thread group (named barrier 1 + g; 0 is __syncthreads).
+// Immediate ids, so that the kernel reserves only the barriers it uses.
+__device__ __forceinline__ void group_sync(uint32_t g) {
+  if (g == 0) asm volatile("bar.sync 1, 128;" ::: "memory");
+  else asm volatile("bar.sync 2, 128;" ::: "memory");
 }
 
-// Waits for the committed MMAs; false (uniformly) when the wait gave up.
-__device__ __forceinline__ bool wait_mma(uint32_t mbar, uint32_t &phase, int *abort, int *err) {
+// Every thread of the group: shared-memory writes visible to the tensor core,
+// TMEM reads done before the next MMA overwrites the accumulator.
+__device__ __forceinline__ void sync_for_mma(uint32_t g) {
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  group_sync(g);
+}
+
+// Waits for the group's committed MMAs; false (uniformly within the group) when
+// the wait gave up.
+__device__ __forceinline__ bool wait_mma(uint32_t g, uint32_t mbar, uint32_t &phase, int *abort, int *err) {
   if (!tc::mbar_wait(mbar, phase, kWaitTries)) {
     *abort = 1;
     atomicExch(err, CKR_ERR_ITERATION_LIMIT);
   }
-  __syncthreads();
+  group_sync(g);
   if (*abort) {
     tc::mbar_wait(mbar, phase, kWaitTries);  // let the MMAs in flight land before TMEM is freed
     return false;
@@ -154,102 +204,154 @@ __device__ __forceinline__ bool wait_mma(uint32_t mbar, uint32_t &phase, int *ab
 }
 
 // ---- inference ------------------------------------------------------------------
+// kGroups independent 128-thread groups per CTA share the weights in shared memory;
+// each owns a 128-row tile, an activation buffer, an mbarrier and 64 TMEM columns,
+// so one group's epilogue overlaps another's MMAs.
+constexpr uint32_t kGroups = 2, kInferTPB = 128 * kGroups;
+
 struct SmemInfer {
   uint8_t w[kImgForward];
-  uint8_t a[128 * kIn * 2];
-  float b[3][64];
-  uint64_t mbar;
+  uint8_t a[kGroups][128 * kIn * 2];
+  uint64_t mbar[kGroups];
   uint32_t tmem;
-  int abort;
+  int abort[kGroups];
 };
 
-__global__ void __launch_bounds__(kTPB) k_mlp_infer(const float4 *__restrict__ rec, uint32_t n_max,
-                                                    const uint32_t *n_dev, uint32_t n_off,
-                                                    const uint8_t *__restrict__ img,
-                                                    const float *__restrict__ params, Params p,
-                                                    __half *__restrict__ probs, int *err) {
+// Network input of one row: a 12-float record, or (PATHS) the shading point of
+// queue entry `row` of the renderer (zeros where the entry is not a shaded surface).
+template <bool PATHS>
+__device__ __forceinline__ void load_row(const float4 *rec, const PathRows &pr, uint32_t row, float4 &r0, float4 &r1,
+                                         float4 &r2) {
+  r0 = r1 = r2 = make_float4(0, 0, 0, 0);
+  if (!PATHS) {
+    r0 = rec[3 * (size_t)row];
+    r1 = rec[3 * (size_t)row + 1];
+    r2 = rec[3 * (size_t)row + 2];
+    return;
+  }
+  const uint32_t slot = pr.queue[row], id = pr.hit_id[slot];
+  const uint4 meta = pr.meta[slot];
+  if (id == kMiss || (meta.w & 1u)) return;
+  const float4 ro = pr.ray_o[slot], rd = pr.ray_d[slot];
+  Surface S = make_surface(pr.sv, f3(ro.x, ro.y, ro.z), f3(rd.x, rd.y, rd.z), id, pr.hit_t[slot]);
+  const ckr_material &mm = pr.sv.mats[S.mat];
+  if (mm.light_type != 0) return;
+  r0 = make_float4(S.x.x, S.x.y, S.x.z, mm.alpha);
+  r1 = make_float4(S.n.x, S.n.y, S.n.z, 0.f);
+  r2 = make_float4(S.wo.x, S.wo.y, S.wo.z, 0.f);
+}
+
+template <bool PATHS>
+__global__ void __launch_bounds__(kInferTPB) k_mlp_infer(const float4 *__restrict__ rec, PathRows pr, uint32_t n_max,
+                                                         const uint32_t *n_dev, uint32_t n_off,
+                                                         const uint8_t *__restrict__ img, Params p, float delta,
+                                                         __half *__restrict__ probs, uint16_t *__restrict__ cdf16,
+                                                         int *err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   SmemInfer &S = *reinterpret_cast<SmemInfer *>(smem_raw);
-  const uint32_t t = threadIdx.x, warp = t >> 5;
-  for (uint32_t i = t; i < kImgForward / 16; i += kTPB)
+  const uint32_t g = threadIdx.x >> 7, t = threadIdx.x & 127u, warp = threadIdx.x >> 5;
+  for (uint32_t i = threadIdx.x; i < kImgForward / 16; i += kInferTPB)
     reinterpret_cast<uint4 *>(S.w)[i] = reinterpret_cast<const uint4 *>(img)[i];
-  for (uint32_t i = t; i < 64; i += kTPB) {
-    S.b[0][i] = params[kOffB2 + i];
-    S.b[1][i] = params[kOffB3 + i];
-    S.b[2][i] = params[kOffB4 + i];
-  }
-  const uint32_t mbar = tc::smem_u32(&S.mbar);
+  const uint32_t mbar = tc::smem_u32(&S.mbar[g]);
   if (t == 0) {
     tc::mbar_init(mbar, 1);
-    S.abort = 0;
+    S.abort[g] = 0;
   }
-  if (warp == 0) tc::tmem_alloc(&S.tmem, 64);
+  if (warp == 0) tc::tmem_alloc(&S.tmem, 64 * kGroups);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  const uint32_t tmem = S.tmem, lane_addr = tmem + ((warp * 32u) << 16);
+  // Warp w reads TMEM lanes 32 (w % 4) .. +31; group g owns columns 64 g .. +63.
+  const uint32_t tmem = S.tmem + 64u * g, lane_addr = tmem + (((warp & 3u) * 32u) << 16);
   const uint32_t n = rows(n_max, n_dev, n_off);
-  const uint32_t a_addr = tc::smem_u32(S.a), w_addr = tc::smem_u32(S.w);
+  uint8_t *A = S.a[g];
+  const uint32_t a_addr = tc::smem_u32(A), w_addr = tc::smem_u32(S.w);
   uint32_t phase = 0;
-  for (uint32_t tile = blockIdx.x; tile * 128u < n; tile += gridDim.x) {
+  for (uint32_t tile = blockIdx.x * kGroups + g; tile * 128u < n; tile += gridDim.x * kGroups) {
     const uint32_t row = tile * 128u + t;
     float4 r0 = make_float4(0, 0, 0, 0), r1 = r0, r2 = r0;
-    if (row < n) {
-      r0 = rec[3 * (size_t)row];
-      r1 = rec[3 * (size_t)row + 1];
-      r2 = rec[3 * (size_t)row + 2];
-    }
-    write_features(S.a, t, r0, r1, r2, p);
-    sync_for_mma();
-    if (t == 0) {
-      tc::fence_after_sync();
-      issue(tmem, a_addr, w_addr + kImgW1, kIn, 0);
-      tc::mma_commit(mbar);
-    }
-    if (!wait_mma(mbar, phase, &S.abort, err)) break;
-    epilogue_relu(lane_addr, nullptr, S.a, t);
+    if (row < n) load_row<PATHS>(rec, pr, row, r0, r1, r2);
+    write_features(A, t, r0, r1, r2, p);
     bool ok = true;
-    for (int l = 0; l < 3 && ok; ++l) {
-      sync_for_mma();
+    for (int l = 0; l < 4 && ok; ++l) {
+      sync_for_mma(g);
       if (t == 0) {
         tc::fence_after_sync();
-        issue(tmem, a_addr, w_addr + kImgW2 + 8192u * l, 64, 0);
+        if (l == 0) issue(tmem, a_addr, w_addr + kImgW1, kIn, 0);
+        else issue(tmem, a_addr, w_addr + kImgW2 + 10240u * (l - 1), kHidK, 0);
         tc::mma_commit(mbar);
       }
-      ok = wait_mma(mbar, phase, &S.abort, err);
-      if (ok && l < 2) epilogue_relu(lane_addr, S.b[l], S.a, t);
+      ok = wait_mma(g, mbar, phase, &S.abort[g], err);
+      if (ok && l < 3) epilogue_relu(lane_addr, A, t);
     }
     if (!ok) break;
-    float pr[64];
-    softmax_row(lane_addr, S.b[2], p.nclusters, pr);
-    if (row < n) {
+    float e[64];
+    const bool full = p.nclusters == 64;
+    const float sum = full ? softmax_exp64(lane_addr, e) : softmax_exp(lane_addr, p.nclusters, e);
+    if (row < n && cdf16 && full) {
+      const float unif = delta / 64.0f, keep = (1.0f - delta) / sum;
+      float run = 0.f;
+      uint32_t w[32];
+#pragma unroll
+      for (int j = 0; j < 64; j += 2) {
+        run += fmaf(keep, e[j], unif);
+        const uint32_t c0 = min(65535u, __float2uint_rn(65535.0f * run));
+        run += fmaf(keep, e[j + 1], unif);
+        const uint32_t c1 = j + 2 == 64 ? 65535u : min(65535u, __float2uint_rn(65535.0f * run));
+        w[j / 2] = c0 | (c1 << 16);
+      }
+      uint4 *dst = reinterpret_cast<uint4 *>(cdf16 + 64 * (size_t)row);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) dst[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+    } else if (row < n && cdf16) {
+      // Selection mixture (1 - delta) softmax + delta / C as a 16-bit cumulative
+      // table: entry j = round(65535 * sum_{i <= j} q_i), the last cluster's 65535.
+      const float unif = delta / (float)p.nclusters, keep = (1.0f - delta) / sum;
+      float run = 0.f;
+      uint32_t w[32];
+#pragma unroll
+      for (int j = 0; j < 64; j += 2) {
+        run += (uint32_t)j < p.nclusters ? keep * e[j] + unif : 0.f;
+        uint32_t c0 = (uint32_t)j + 1 >= p.nclusters ? 65535u : min(65535u, __float2uint_rn(65535.0f * run));
+        run += (uint32_t)j + 1 < p.nclusters ? keep * e[j + 1] + unif : 0.f;
+        uint32_t c1 = (uint32_t)j + 2 >= p.nclusters ? 65535u : min(65535u, __float2uint_rn(65535.0f * run));
+        w[j / 2] = c0 | (c1 << 16);
+      }
+      uint4 *dst = reinterpret_cast<uint4 *>(cdf16 + 64 * (size_t)row);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) dst[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+    }
+    if (row < n && probs) {
+      const float inv = 1.0f / sum;
       uint4 *dst = reinterpret_cast<uint4 *>(probs + 64 * (size_t)row);
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        __half2 h0 = __floats2half2_rn(pr[8 * q], pr[8 * q + 1]), h1 = __floats2half2_rn(pr[8 * q + 2], pr[8 * q + 3]);
-        __half2 h2 = __floats2half2_rn(pr[8 * q + 4], pr[8 * q + 5]), h3 = __floats2half2_rn(pr[8 * q + 6], pr[8 * q + 7]);
+        const float *x = e + 8 * q;
+        __half2 h0 = __floats2half2_rn(x[0] * inv, x[1] * inv), h1 = __floats2half2_rn(x[2] * inv, x[3] * inv);
+        __half2 h2 = __floats2half2_rn(x[4] * inv, x[5] * inv), h3 = __floats2half2_rn(x[6] * inv, x[7] * inv);
         dst[q] = make_uint4(*reinterpret_cast<uint32_t *>(&h0), *reinterpret_cast<uint32_t *>(&h1),
                             *reinterpret_cast<uint32_t *>(&h2), *reinterpret_cast<uint32_t *>(&h3));
       }
     }
     tc::fence_before_sync();
-    __syncthreads();
+    group_sync(g);
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+  if (warp == 0) tc::tmem_dealloc(S.tmem, 64 * kGroups);
 }
 
 // ---- training -------------------------------------------------------------------
+constexpr uint32_t kTrainTPB = 128;
+
 struct SmemTrain {
   uint8_t w[kImgBytes];
   uint8_t x0[128 * kIn * 2];
-  uint8_t h[3][128 * 64 * 2];
-  uint8_t g[128 * 64 * 2];   // G [128 rows x K 64]
-  uint8_t gt[64 * 128 * 2];  // G^T [64 x K 128]
-  uint8_t ht[128 * 128 * 2]; // X^T [128 (features, padded) x K 128]
-  float b[3][64];
-  float loss[kTPB / 32];
+  uint8_t h[3][128 * kHidK * 2];  // H1, H2, H3 with the constant-1 column (K = 80)
+  uint8_t g[128 * 64 * 2];        // G [128 rows x K 64]
+  uint8_t gt[64 * 128 * 2];       // G^T [64 x K 128]
+  uint8_t ht[128 * 128 * 2];      // X^T [128 (features, padded) x K 128]
+  float loss[kTrainTPB / 32];
   uint64_t mbar;
   uint32_t tmem;
   int abort;
@@ -259,23 +361,18 @@ constexpr uint32_t kColD = 0;
 // TMEM column of the dW^T accumulator of layer l = 0..3 (dW1..dW4).
 __device__ __forceinline__ uint32_t col_w(int l) { return 256u - 64u * (uint32_t)l; }
 
-__global__ void __launch_bounds__(kTPB) k_mlp_train(const float4 *__restrict__ rec, uint32_t n_max,
-                                                    const uint32_t *n_dev, uint32_t n_off,
-                                                    const uint8_t *__restrict__ img,
-                                                    const float *__restrict__ params, const float *scalars,
-                                                    Params p, float *__restrict__ part, float *loss_part,
-                                                    int *err) {
+__global__ void __launch_bounds__(kTrainTPB) k_mlp_train(const float4 *__restrict__ rec, uint32_t n_max,
+                                                         const uint32_t *n_dev, uint32_t n_off,
+                                                         const uint8_t *__restrict__ img, const float *scalars,
+                                                         Params p, float *__restrict__ part, float *loss_part,
+                                                         int *err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   SmemTrain &S = *reinterpret_cast<SmemTrain *>(smem_raw);
   const uint32_t t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  for (uint32_t i = t; i < kImgBytes / 16; i += kTPB)
+  for (uint32_t i = t; i < kImgBytes / 16; i += kTrainTPB)
     reinterpret_cast<uint4 *>(S.w)[i] = reinterpret_cast<const uint4 *>(img)[i];
-  for (uint32_t i = t; i < sizeof(S.ht) / 16; i += kTPB) reinterpret_cast<uint4 *>(S.ht)[i] = make_uint4(0, 0, 0, 0);
-  for (uint32_t i = t; i < 64; i += kTPB) {
-    S.b[0][i] = params[kOffB2 + i];
-    S.b[1][i] = params[kOffB3 + i];
-    S.b[2][i] = params[kOffB4 + i];
-  }
+  for (uint32_t i = t; i < sizeof(S.ht) / 16; i += kTrainTPB)
+    reinterpret_cast<uint4 *>(S.ht)[i] = make_uint4(0, 0, 0, 0);
   const uint32_t mbar = tc::smem_u32(&S.mbar);
   if (t == 0) {
     tc::mbar_init(mbar, 1);
@@ -290,7 +387,7 @@ __global__ void __launch_bounds__(kTPB) k_mlp_train(const float4 *__restrict__ r
   const float wsum = scalars[0];
   const uint32_t w_addr = tc::smem_u32(S.w), x0_addr = tc::smem_u32(S.x0), g_addr = tc::smem_u32(S.g),
                  gt_addr = tc::smem_u32(S.gt), ht_addr = tc::smem_u32(S.ht);
-  const uint32_t h0_addr = tc::smem_u32(S.h[0]);  // H1, H2, H3 are 16 KB apart
+  const uint32_t h0_addr = tc::smem_u32(S.h[0]);  // H1, H2, H3 are 20 KB apart
   uint32_t phase = 0, tiles = 0;
   float loss = 0.f;
   bool ok = wsum > 0.f;
@@ -307,32 +404,28 @@ __global__ void __launch_bounds__(kTPB) k_mlp_train(const float4 *__restrict__ r
     const uint32_t acc = tiles ? 1u : 0u;
     // ---- forward ----
     write_features(S.x0, t, r0, r1, r2, p);
-    sync_for_mma();
-    if (t == 0) {
-      tc::fence_after_sync();
-      issue(tmem + kColD, x0_addr, w_addr + kImgW1, kIn, 0);
-      tc::mma_commit(mbar);
-    }
-    if (!(ok = wait_mma(mbar, phase, &S.abort, err))) break;
-    epilogue_relu(lane_addr + kColD, nullptr, S.h[0], t);
-    for (int l = 0; l < 3 && ok; ++l) {
-      sync_for_mma();
+    for (int l = 0; l < 4 && ok; ++l) {
+      sync_for_mma(0);
       if (t == 0) {
         tc::fence_after_sync();
-        issue(tmem + kColD, h0_addr + 16384u * l, w_addr + kImgW2 + 8192u * l, 64, 0);
+        if (l == 0) issue(tmem + kColD, x0_addr, w_addr + kImgW1, kIn, 0);
+        else issue(tmem + kColD, h0_addr + 20480u * (l - 1), w_addr + kImgW2 + 10240u * (l - 1), kHidK, 0);
         tc::mma_commit(mbar);
       }
-      ok = wait_mma(mbar, phase, &S.abort, err);
-      if (ok && l < 2) epilogue_relu(lane_addr + kColD, S.b[l], S.h[l + 1], t);
+      ok = wait_mma(0, mbar, phase, &S.abort, err);
+      if (ok && l < 3) epilogue_relu(lane_addr + kColD, S.h[l], t);
     }
     if (!ok) break;
-    // ---- loss gradient at the logits ----
+    // ---- loss gradient at the logits: a (softmax - onehot(k)) ----
     {
       float pr[64];
-      softmax_row(lane_addr + kColD, S.b[2], p.nclusters, pr);
+      const float inv = 1.0f / softmax_exp(lane_addr + kColD, p.nclusters, pr);
       float pk = 0.f;
 #pragma unroll
-      for (int j = 0; j < 64; ++j) pk = (uint32_t)j == k ? pr[j] : pk;
+      for (int j = 0; j < 64; ++j) {
+        pr[j] *= inv;
+        pk = (uint32_t)j == k ? pr[j] : pk;
+      }
       if (a > 0.f) loss -= a * __logf(fmaxf(pk, 1e-30f));
 #pragma unroll
       for (int j = 0; j < 64; ++j) pr[j] = (uint32_t)j < p.nclusters ? a * (pr[j] - ((uint32_t)j == k ? 1.f : 0.f)) : 0.f;
@@ -341,33 +434,33 @@ __global__ void __launch_bounds__(kTPB) k_mlp_train(const float4 *__restrict__ r
 #pragma unroll
       for (int j = 0; j < 64; ++j) st1(S.gt, j, t, 128, pr[j]);
     }
-    // ---- backward, layers 4, 3, 2 ----
+    // ---- backward, layers 4, 3, 2 (input H3, H2, H1) ----
     for (int l = 2; l >= 0 && ok; --l) {
-      // X^T of this layer's input (H3, H2, H1) with the ones row for the bias.
+      // X^T of the layer's input with the ones row (64) for the bias.
       {
         float v[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-          ld8(S.h[l], t, 8 * q, 64, v);
+          ld8(S.h[l], t, 8 * q, kHidK, v);
 #pragma unroll
           for (int j = 0; j < 8; ++j) st1(S.ht, 8 * q + j, t, 128, v[j]);
         }
         st1(S.ht, 64, t, 128, 1.0f);
       }
-      sync_for_mma();
+      sync_for_mma(0);
       if (t == 0) {
         tc::fence_after_sync();
-        issue(tmem + col_w(l + 1), ht_addr, gt_addr, 128, acc);  // dW^T += X^T G
+        issue(tmem + col_w(l + 1), ht_addr, gt_addr, 128, acc);            // dW^T += X^T G
         issue(tmem + kColD, g_addr, w_addr + kImgW2t + 8192u * l, 64, 0);  // dX = G W
         tc::mma_commit(mbar);
       }
-      if (!(ok = wait_mma(mbar, phase, &S.abort, err))) break;
+      if (!(ok = wait_mma(0, mbar, phase, &S.abort, err))) break;
       // G of the layer below: dX masked by its ReLU.
       float d[64], hv[64];
       tc::tmem_ld32(lane_addr + kColD, d);
       tc::tmem_ld32(lane_addr + kColD + 32, d + 32);
 #pragma unroll
-      for (int q = 0; q < 8; ++q) ld8(S.h[l], t, 8 * q, 64, hv + 8 * q);
+      for (int q = 0; q < 8; ++q) ld8(S.h[l], t, 8 * q, kHidK, hv + 8 * q);
 #pragma unroll
       for (int j = 0; j < 64; ++j) d[j] = hv[j] > 0.f ? d[j] : 0.f;
       if (l > 0) {
@@ -388,13 +481,13 @@ __global__ void __launch_bounds__(kTPB) k_mlp_train(const float4 *__restrict__ r
         for (int j = 0; j < 8; ++j) st1(S.ht, 8 * q + j, t, 128, v[j]);
       }
     }
-    sync_for_mma();
+    sync_for_mma(0);
     if (t == 0) {
       tc::fence_after_sync();
       issue(tmem + col_w(0), ht_addr, gt_addr, 128, acc);
       tc::mma_commit(mbar);
     }
-    if (!(ok = wait_mma(mbar, phase, &S.abort, err))) break;
+    if (!(ok = wait_mma(0, mbar, phase, &S.abort, err))) break;
     tc::fence_before_sync();
     __syncthreads();
   }
@@ -464,12 +557,15 @@ __device__ __forceinline__ void image_slots(uint32_t j, int &a, int &b) {
   } else {
     const uint32_t offs[3] = {kOffW2, kOffW3, kOffW4}, img[3] = {kImgW2, kImgW3, kImgW4},
                    imgt[3] = {kImgW2t, kImgW3t, kImgW4t};
-    for (int l = 0; l < 3; ++l)
+    for (int l = 0; l < 3; ++l) {
       if (j >= offs[l] && j < offs[l] + 4096) {
         uint32_t o = (j - offs[l]) / 64, i = (j - offs[l]) % 64;
-        a = img[l] + tc::kmaj(o, i, 64);
+        a = img[l] + tc::kmaj(o, i, kHidK);
         b = imgt[l] + tc::kmaj(i, o, 64);
+      } else if (j >= offs[l] + 4096 && j < offs[l] + 4096 + 64) {  // bias of output o at K = 64
+        a = img[l] + tc::kmaj(j - offs[l] - 4096, 64, kHidK);
       }
+    }
   }
 }
 
@@ -556,7 +652,10 @@ int create(Net &net, uint64_t seed) {
   CKR_CUDA_TRY(cudaMemset(net.err, 0, 4));
   int dev = 0;
   CKR_CUDA_TRY(cudaGetDevice(&dev));
-  CKR_CUDA_TRY(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemInfer)));
+  for (const void *fn : {(const void *)k_mlp_infer<false>, (const void *)k_mlp_infer<true>}) {
+    CKR_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemInfer)));
+    CKR_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  }
   CKR_CUDA_TRY(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemTrain)));
   int st = pack(net, nullptr);
   if (st != CKR_OK) return st;
@@ -584,23 +683,42 @@ int pack(Net &net, cudaStream_t stream) {
   return CKR_OK;
 }
 
-int infer(const Net &net, const float4 *rec, uint32_t n_max, const uint32_t *n_dev, __half *probs,
-          cudaStream_t stream) {
+namespace {
+template <bool PATHS>
+int launch_infer(const Net &net, const float4 *rec, const PathRows &pr, uint32_t n_max, const uint32_t *n_dev,
+                 __half *probs, uint16_t *cdf16, float delta, cudaStream_t stream) {
   if (n_max == 0) return CKR_OK;
-  int per = 0;
-  CKR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mlp_infer, kTPB, sizeof(SmemInfer)));
-  uint32_t grid = std::min<uint32_t>(ceil_div(n_max, 128), (uint32_t)sm_count() * std::max(1, per));
-  k_mlp_infer<<<grid, kTPB, sizeof(SmemInfer), stream>>>(rec, n_max, n_dev, 0, net.img, net.params, params_of(net),
-                                                        probs, net.err);
+  // CTAs resident per SM: shared memory (the opt-in maximum over the CTA's
+  // footprint plus the 1 KB the driver reserves per CTA) or 4.
+  static int per_sm = 0;
+  if (!per_sm) {
+    int dev = 0, smem = 0;
+    CKR_CUDA_TRY(cudaGetDevice(&dev));
+    CKR_CUDA_TRY(cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    per_sm = std::max(1, std::min(4, smem / (int)(sizeof(SmemInfer) + 1024)));
+  }
+  uint32_t grid = std::min<uint32_t>(ceil_div(n_max, 128 * kGroups), (uint32_t)sm_count() * per_sm);
+  k_mlp_infer<PATHS><<<grid, kInferTPB, sizeof(SmemInfer), stream>>>(rec, pr, n_max, n_dev, 0, net.img,
+                                                                    params_of(net), delta, probs, cdf16, net.err);
   CKR_CUDA_TRY(cudaGetLastError());
   return CKR_OK;
+}
+}  // namespace
+
+int infer(const Net &net, const float4 *rec, uint32_t n_max, const uint32_t *n_dev, __half *probs, uint16_t *cdf16,
+          float delta, cudaStream_t stream) {
+  return launch_infer<false>(net, rec, PathRows{}, n_max, n_dev, probs, cdf16, delta, stream);
+}
+
+int infer_paths(const Net &net, const PathRows &rows, uint32_t n_max, const uint32_t *n_dev, uint16_t *cdf16,
+                float delta, cudaStream_t stream) {
+  return launch_infer<true>(net, nullptr, rows, n_max, n_dev, nullptr, cdf16, delta, stream);
 }
 
 int gradients(Net &net, const float4 *rec, uint32_t n_max, const uint32_t *n_dev, uint32_t n_off,
               cudaStream_t stream) {
   k_mlp_wsum<<<1, 1024, 0, stream>>>(rec, n_max, n_dev, n_off, net.scalars);
-  k_mlp_train<<<net.grid, kTPB, sizeof(SmemTrain), stream>>>(rec, n_max, n_dev, n_off, net.img, net.params,
-                                                            net.scalars,
+  k_mlp_train<<<net.grid, kTrainTPB, sizeof(SmemTrain), stream>>>(rec, n_max, n_dev, n_off, net.img, net.scalars,
                                                             params_of(net), net.part, net.loss_part, net.err);
   CKR_CUDA_TRY(cudaGetLastError());
   return CKR_OK;

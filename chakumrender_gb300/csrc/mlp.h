@@ -12,17 +12,32 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "scene.h"
+
 namespace ckr {
 namespace mlp {
+
+// Network input straight from the renderer's path state: queue entry i is path
+// slot queue[i]; its shading point comes from the hit record and the scene.
+struct PathRows {
+  const uint32_t *queue = nullptr, *hit_id = nullptr;
+  const float4 *ray_o = nullptr, *ray_d = nullptr;
+  const float *hit_t = nullptr;
+  const uint4 *meta = nullptr;
+  ShadeView sv{};
+};
 
 constexpr uint32_t kIn = 96, kHid = 64, kOut = 64, kFreqs = 12;
 constexpr uint32_t kOffW1 = 0, kOffW2 = kOffW1 + kHid * kIn, kOffB2 = kOffW2 + kHid * kHid,
                    kOffW3 = kOffB2 + kHid, kOffB3 = kOffW3 + kHid * kHid, kOffW4 = kOffB3 + kHid,
                    kOffB4 = kOffW4 + kOut * kHid, kNParams = kOffB4 + kOut;
-// BF16 operand images (K-major core-matrix layout): W1 [64 x 96], W2, W3, W4
-// [64 x 64], then the transposes W2t, W3t, W4t used by the backward pass.
-constexpr uint32_t kImgW1 = 0, kImgW2 = 12288, kImgW3 = 20480, kImgW4 = 28672, kImgW2t = 36864, kImgW3t = 45056,
-                   kImgW4t = 53248, kImgForward = 36864, kImgBytes = 61440;
+// BF16 operand images (K-major core-matrix layout): W1 [64 x 96] (its bias is the
+// weight of the constant feature 79); W2, W3, W4 [64 x 80]: the 64 weights of an
+// output, its bias at K = 64 (the activations carry a constant 1 there) and zeros;
+// then the transposes W2t, W3t, W4t [64 x 64] used by the backward pass.
+constexpr uint32_t kHidK = 80;  // K of the hidden-layer operands
+constexpr uint32_t kImgW1 = 0, kImgW2 = 12288, kImgW3 = 22528, kImgW4 = 32768, kImgW2t = 43008, kImgW3t = 51200,
+                   kImgW4t = 59392, kImgForward = 43008, kImgBytes = 67584;
 
 struct Net {
   float *params = nullptr, *m = nullptr, *v = nullptr;  // FP32 master weights and Adam moments
@@ -40,10 +55,15 @@ struct Net {
 
 int create(Net &net, uint64_t seed);
 void destroy(Net &net);
-// Probabilities (FP16, 64 per row) for rows [0, n), n = min(*n_dev, n_max) when
-// n_dev is not null, else n_max.  rec: 3 float4 per row.
-int infer(const Net &net, const float4 *rec, uint32_t n_max, const uint32_t *n_dev, __half *probs,
-          cudaStream_t stream);
+// Network output for rows [0, n), n = min(*n_dev, n_max) when n_dev is not null,
+// else n_max; rec: 3 float4 per row.  probs (nullable): the softmax, FP16, 64 per
+// row.  cdf16 (nullable): the selection mixture (1 - delta) softmax + delta / C as
+// 64 cumulative 16-bit entries per row, pmf(j) = (cdf[j] - cdf[j-1]) / 65535.
+int infer(const Net &net, const float4 *rec, uint32_t n_max, const uint32_t *n_dev, __half *probs, uint16_t *cdf16,
+          float delta, cudaStream_t stream);
+// The selection CDFs for the renderer's queue entries [0, min(*n_dev, n_max)).
+int infer_paths(const Net &net, const PathRows &rows, uint32_t n_max, const uint32_t *n_dev, uint16_t *cdf16,
+                float delta, cudaStream_t stream);
 // One Adam step on the records [0, n) of rec, n = min(*n_dev - n_off, n_max) (rec
 // already advanced by n_off rows) or n_max; skipped (no update) when their weights
 // sum to 0.

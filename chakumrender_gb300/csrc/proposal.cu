@@ -39,6 +39,7 @@ extern "C" int ckr_proposal_create(const ckr_scene *s, const ckr_proposal_cfg *c
   p->defensive = c.defensive;
   p->batch = c.batch;
   p->minibatch = c.minibatch;
+  p->max_steps = c.max_steps;
   p->train = c.train ? 1 : 0;
   int st = mlp::create(p->net, c.seed);
   if (st == CKR_OK && p->rec_count.reserve(1) != cudaSuccess) st = CKR_ERR_OUT_OF_MEMORY;
@@ -101,7 +102,7 @@ extern "C" int ckr_proposal_infer(ckr_proposal *p, const float *rec12, uint32_t 
     return CKR_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lock(p->mu);
   return mlp::infer(p->net, reinterpret_cast<const float4 *>(rec12), n, nullptr, reinterpret_cast<__half *>(probs),
-                    (cudaStream_t)stream);
+                    nullptr, p->defensive, (cudaStream_t)stream);
 }
 
 extern "C" int ckr_proposal_train_step(ckr_proposal *p, const float *rec12, uint32_t n, void *stream) {

@@ -15,11 +15,11 @@ struct ckr_proposal {
   float defensive = 0.2f;   // uniform fraction of the selection mixture
   uint32_t batch = 65536;      // training records kept per bounce
   uint32_t minibatch = 16384;  // records per Adam step (batch / minibatch steps per bounce)
+  uint32_t max_steps = 0;      // training stops after this many Adam steps (0: never)
   int train = 1;
   std::mutex mu;
   // Renderer buffers, grown on demand.
-  ckr::DevBuf<float4> mlp_in;     // network input rows of one bounce (3 float4 each)
-  ckr::DevBuf<__half> probs[2];   // network output of the current / previous bounce
+  ckr::DevBuf<uint16_t> sel[2];   // selection CDFs of the current / previous bounce (64 x u16 per row)
   ckr::DevBuf<float4> rec;        // training records (3 float4 each)
   ckr::DevBuf<uint32_t> rec_count;
   ckr::DevBuf<uint32_t> prev_row, sh_rec;

@@ -38,9 +38,8 @@ constexpr uint32_t kNoRec = 0xFFFFFFFFu;
 // Hooks of the learned light selection (CKR_SHADER_PATH_NEE with a proposal
 // network); all null for selection in proportion to power.
 struct Learn {
-  const __half *probs;       // [queue row x 64] network output at this bounce's vertices
-  const __half *probs_prev;  // the same at the previous bounce (rows by Paths::prev_row)
-  float delta;               // defensive fraction of the uniform distribution
+  const uint16_t *sel;       // [queue row x 64] selection CDFs at this bounce's vertices
+  const uint16_t *sel_prev;  // the same at the previous bounce (rows by Paths::prev_row)
   float4 *rec;               // training records, 3 float4 each: (x, alpha), (n, value), (wo, cluster)
   uint32_t *rec_count;
   uint32_t rec_cap;
@@ -446,8 +445,7 @@ __global__ void __launch_bounds__(kRTPB) k_shade_nee(ShadeView sv, Paths P, Para
             uint32_t k = (id & kSphereBit) ? kNoLight : __ldg(&sv.tri_light[id]);
             if (k != kNoLight && b4.w > 0.f) {
               DevLight L = sv.lights[k];
-              Select sel = make_select(sv, lr.probs_prev ? lr.probs_prev + 64 * (size_t)P.prev_row[slot] : nullptr,
-                                       lr.delta);
+              Select sel{lr.sel_prev ? lr.sel_prev + 64 * (size_t)P.prev_row[slot] : nullptr};
               const float *t9 = sv.tri9 + 9 * (size_t)id;
               F3 A = f3(__ldg(t9), __ldg(t9 + 1), __ldg(t9 + 2));
               F3 B = f3(__ldg(t9 + 3), __ldg(t9 + 4), __ldg(t9 + 5));
@@ -468,7 +466,7 @@ __global__ void __launch_bounds__(kRTPB) k_shade_nee(ShadeView sv, Paths P, Para
           // ---- light technique: one sample ----
           float e0 = ckr_draw_f(key, ctr(meta.y, meta.z, 0)), e1 = ckr_draw_f(key, ctr(meta.y, meta.z, 1));
           float e2 = ckr_draw_f(key, ctr(meta.y, meta.z, 2)), e3 = ckr_draw_f(key, ctr(meta.y, meta.z, 3));
-          Select sel = make_select(sv, lr.probs ? lr.probs + 64 * (size_t)i : nullptr, lr.delta);
+          Select sel{lr.sel ? lr.sel + 64 * (size_t)i : nullptr};
           uint32_t j = select_pick(sv, sel, e0);
           DevLight L = sv.lights[sv.first_emit + j];
           uint32_t tri = L.first + cdf_pick(sv.pcdf + L.pcdf, L.count, e1);
@@ -556,34 +554,9 @@ __global__ void __launch_bounds__(kRTPB) k_shade_nee(ShadeView sv, Paths P, Para
       P.beta[slot] = next_b;
       uint32_t nd = meta.z + 1;
       P.meta[slot] = make_uint4(meta.x, meta.y, nd, nd >= prm.max_depth ? 1u : 0u);
-      if (lr.probs) P.prev_row[slot] = i;
+      if (lr.sel) P.prev_row[slot] = i;
       qn[cbase] = slot;
     }
-  }
-}
-
-// Network input rows of the learned selection, one per queue entry (zeros for
-// entries that are not shaded surfaces).
-__global__ void __launch_bounds__(kRTPB) k_nee_prep(ShadeView sv, Paths P, int cur, float4 *mlp_in) {
-  const uint32_t n = P.counts[cur];
-  const uint32_t *q = cur ? P.q1 : P.q0;
-  for (uint32_t i = blockIdx.x * kRTPB + threadIdx.x; i < n; i += gridDim.x * kRTPB) {
-    const uint32_t slot = q[i], id = P.hit_id[slot];
-    const uint4 meta = P.meta[slot];
-    float4 a = make_float4(0, 0, 0, 0), b = a, c = a;
-    if (id != kMiss && !(meta.w & 1u)) {
-      float4 ro = P.ray_o[slot], rd = P.ray_d[slot];
-      Surface S = make_surface(sv, f3(ro.x, ro.y, ro.z), f3(rd.x, rd.y, rd.z), id, P.hit_t[slot]);
-      const ckr_material &mm = sv.mats[S.mat];
-      if (mm.light_type == 0) {
-        a = make_float4(S.x.x, S.x.y, S.x.z, mm.alpha);
-        b = make_float4(S.n.x, S.n.y, S.n.z, 0.f);
-        c = make_float4(S.wo.x, S.wo.y, S.wo.z, 0.f);
-      }
-    }
-    mlp_in[3 * (size_t)i] = a;
-    mlp_in[3 * (size_t)i + 1] = b;
-    mlp_in[3 * (size_t)i + 2] = c;
   }
 }
 
@@ -693,11 +666,10 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   P.counts = W.counts.ptr;
   P.stats = W.stats.ptr;
   P.accum = acc;
-  const bool train = prop && prop->train;
+  bool train = prop && prop->train && (!prop->max_steps || prop->net.step < prop->max_steps);
   if (prop) {
-    CKR_CUDA_TRY(prop->mlp_in.reserve(3 * wave));
-    CKR_CUDA_TRY(prop->probs[0].reserve(64 * wave));
-    CKR_CUDA_TRY(prop->probs[1].reserve(64 * wave));
+    CKR_CUDA_TRY(prop->sel[0].reserve(64 * wave));
+    CKR_CUDA_TRY(prop->sel[1].reserve(64 * wave));
     CKR_CUDA_TRY(prop->prev_row.reserve(wave));
     CKR_CUDA_TRY(prop->sh_rec.reserve(shadow));
     CKR_CUDA_TRY(prop->rec.reserve(3 * (size_t)prop->batch));
@@ -737,14 +709,20 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
       CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), stream));
       Learn lr{};
       if (prop) {
-        // Network input for this bounce's vertices, then its light distributions.
-        k_nee_prep<<<g_shade, kRTPB, 0, stream>>>(shv, P, cur, prop->mlp_in.ptr);
-        int ms = mlp::infer(prop->net, prop->mlp_in.ptr, (uint32_t)wave, P.counts + cur, prop->probs[d & 1].ptr,
-                            stream);
+        // Light distributions at this bounce's vertices.
+        mlp::PathRows pr;
+        pr.queue = cur ? P.q1 : P.q0;
+        pr.hit_id = P.hit_id;
+        pr.ray_o = P.ray_o;
+        pr.ray_d = P.ray_d;
+        pr.hit_t = P.hit_t;
+        pr.meta = P.meta;
+        pr.sv = shv;
+        int ms = mlp::infer_paths(prop->net, pr, (uint32_t)wave, P.counts + cur, prop->sel[d & 1].ptr,
+                                  prop->defensive, stream);
         if (ms != CKR_OK) return ms;
-        lr.probs = prop->probs[d & 1].ptr;
-        lr.probs_prev = d ? prop->probs[(d - 1) & 1].ptr : nullptr;
-        lr.delta = prop->defensive;
+        lr.sel = prop->sel[d & 1].ptr;
+        lr.sel_prev = d ? prop->sel[(d - 1) & 1].ptr : nullptr;
         if (train) {
           lr.rec = prop->rec.ptr;
           lr.rec_count = prop->rec_count.ptr;
@@ -769,6 +747,7 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
           if (ts != CKR_OK) return ts;
         }
         CKR_CUDA_TRY(cudaMemsetAsync(prop->rec_count.ptr, 0, 4, stream));
+        if (prop->max_steps && prop->net.step >= prop->max_steps) train = false;  // converged: inference only
       }
       cur ^= 1;
       if (!path) break;

@@ -2,7 +2,6 @@
 // surface interaction, light sampling and the MIS pdf sums of the reference's
 // MIS sampler (src/mis.cpp:18-223), offsets for secondary rays.
 #pragma once
-#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -204,39 +203,29 @@ __device__ __forceinline__ float cdf_mass(const float *cdf, uint32_t j) {
 }
 
 // Light-selection distribution at one vertex over the emitter lights
-// [first_emit, first_emit + n_emit): their power CDF, or the mixture
-// (1 - delta) p / sum(p) + delta / n_emit of a proposal's 64 probabilities p.
+// [first_emit, first_emit + n_emit): their power CDF, or a proposal's 16-bit
+// cumulative table (64 entries; pmf(j) = (cdf[j] - cdf[j-1]) / 65535, the
+// sampler below draws exactly that pmf).
 struct Select {
-  const __half *p;  // nullptr: power
-  float scale, unif;
+  const uint16_t *cdf;  // nullptr: power
 };
 
-__device__ __forceinline__ Select make_select(const ShadeView &sv, const __half *p, float delta) {
-  Select s;
-  s.p = p;
-  s.scale = 0.f;
-  s.unif = 0.f;
-  if (p) {
-    float sum = 0.f;
-    for (uint32_t j = 0; j < sv.n_emit; ++j) sum += __half2float(p[j]);
-    s.scale = sum > 0.f ? (1.0f - delta) / sum : 0.f;
-    s.unif = (sum > 0.f ? delta : 1.0f) / (float)sv.n_emit;
-  }
-  return s;
-}
-
 __device__ __forceinline__ float select_prob(const ShadeView &sv, const Select &s, uint32_t j) {
-  return s.p ? s.scale * __half2float(s.p[j]) + s.unif : cdf_mass(sv.sel_cdf, j);
+  if (!s.cdf) return cdf_mass(sv.sel_cdf, j);
+  const uint32_t hi = __ldg(s.cdf + j), lo = j ? __ldg(s.cdf + j - 1) : 0u;
+  return (float)(hi - lo) * (1.0f / 65535.0f);
 }
 
 __device__ __forceinline__ uint32_t select_pick(const ShadeView &sv, const Select &s, float u) {
-  if (!s.p) return cdf_pick(sv.sel_cdf, sv.n_emit, u);
-  float run = 0.f;
-  for (uint32_t j = 0; j + 1 < sv.n_emit; ++j) {
-    run += s.scale * __half2float(s.p[j]) + s.unif;
-    if (u < run) return j;
+  if (!s.cdf) return cdf_pick(sv.sel_cdf, sv.n_emit, u);
+  const float x = u * 65535.0f;
+  uint32_t lo = 0, hi = sv.n_emit - 1;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (x < (float)__ldg(s.cdf + mid)) hi = mid;
+    else lo = mid + 1;
   }
-  return sv.n_emit - 1;
+  return lo;
 }
 
 // Solid-angle pdf of the light technique for a direction that meets emitter

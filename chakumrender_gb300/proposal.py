@@ -15,7 +15,7 @@ NPARAMS = 18624
 
 class ProposalCfg(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("lr", C.c_float), ("defensive", C.c_float), ("batch", U32), ("train", U32),
-                ("minibatch", U32), ("reserved", U32)]
+                ("minibatch", U32), ("max_steps", U32)]
 
 
 def _sigs():
@@ -40,11 +40,11 @@ class Proposal:
     """Owns a ckr_proposal for a RenderScene."""
 
     def __init__(self, scene: RenderScene, seed=1, lr=1e-3, defensive=0.2, batch=65536, train=True,
-                 minibatch=16384):
+                 minibatch=16384, max_steps=0):
         L = _sigs()
         self.scene = scene
         self._h = P()
-        cfg = ProposalCfg(seed, lr, defensive, batch, 1 if train else 0, min(minibatch, batch))
+        cfg = ProposalCfg(seed, lr, defensive, batch, 1 if train else 0, min(minibatch, batch), max_steps)
         check(L.ckr_proposal_create(scene.handle, C.byref(cfg), C.byref(self._h)), "ckr_proposal_create")
 
     @property

@@ -257,7 +257,7 @@ typedef struct ckr_proposal_cfg {
   uint32_t batch;     /* training records kept per bounce (65536) */
   uint32_t train;     /* 1: train while rendering */
   uint32_t minibatch; /* records per Adam step, batch / minibatch steps per bounce (16384; 0: batch) */
-  uint32_t reserved;
+  uint32_t max_steps; /* training stops after this many Adam steps in total (0: never) */
 } ckr_proposal_cfg;
 #define CKR_PROPOSAL_NPARAMS 18624 /* W1[64][96], W2[64][64], b2, W3, b3, W4, b4 */
 

@@ -21,14 +21,15 @@ def bf16(x):
 
 
 def emulate(params, rec, centre, scale, C):
-    """The kernel's arithmetic in numpy: BF16 features, weights and activations,
-    wide accumulation, FP32-like softmax."""
+    """The kernel's arithmetic in numpy: BF16 features, weights, biases and
+    activations, wide accumulation, softmax."""
     f = bf16(O.mlp_features(rec, centre, scale))
     p = np.asarray(params, np.float64)
     W1 = bf16(p[0:6144].reshape(64, 96))
-    W2, b2 = bf16(p[6144:10240].reshape(64, 64)), p[10240:10304]
-    W3, b3 = bf16(p[10304:14400].reshape(64, 64)), p[14400:14464]
-    W4, b4 = bf16(p[14464:18560].reshape(64, 64)), p[18560:18624]
+    # Biases ride in the weight operands (BF16) against a constant-1 activation.
+    W2, b2 = bf16(p[6144:10240].reshape(64, 64)), bf16(p[10240:10304])
+    W3, b3 = bf16(p[10304:14400].reshape(64, 64)), bf16(p[14400:14464])
+    W4, b4 = bf16(p[14464:18560].reshape(64, 64)), bf16(p[18560:18624])
     h = bf16(np.maximum(f @ W1.T, 0))
     h = bf16(np.maximum(h @ W2.T + b2, 0))
     h = bf16(np.maximum(h @ W3.T + b3, 0))

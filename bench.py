@@ -348,6 +348,65 @@ def bench_manylight(torch):
                          "lr": 1e-3}}
 
 
+def bench_batch(torch):
+    """64 box-scene jobs (random sphere BRDFs GGX/Beckmann/Phong with roughness in
+    [0.05, 0.9], camera yaw in [-30, 30] degrees, resolution from {256..1024}^2, spp
+    from {4, 16, 64}, depth from {3, 6}), path tracer with MIS: one wavefront pass
+    replayed from a CUDA graph (block and wave sizes from the autotuner) against the
+    same jobs rendered one after another with their own launches."""
+    from chakumrender_gb300 import scene as S
+    from chakumrender_gb300.batch import Batch, Job, box_jobs
+
+    sd = S.load_xml(S.SCENES / "box.xml")
+    params, mats = box_jobs(sd, njobs=64, seed=4)
+    outs = [torch.empty((p["cam"].height, p["cam"].width, 3), dtype=torch.float32, device="cuda") for p in params]
+    jobs = [Job(p["cam"], p["spp"], p["max_depth"], p["seed"], p["material_set"], 0, o.data_ptr())
+            for p, o in zip(params, outs)]
+    scene = S.RenderScene(sd)
+    t0 = time.perf_counter()
+    b = Batch(scene, jobs, materials=mats, shader=S.SHADER_PATH)
+    create_s = time.perf_counter() - t0
+    paths, launches = b.stats()
+    tune = b.tuning()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    s = torch.cuda.current_stream()
+    b.render(s.cuda_stream)
+    b.render_sequential(s.cuda_stream)
+    ev[0].record(s)
+    b.render(s.cuda_stream)
+    ev[1].record(s)
+    b.render_sequential(s.cuda_stream)
+    ev[2].record(s)
+    torch.cuda.synchronize()
+    t_graph = ev[0].elapsed_time(ev[1]) / 1e3
+    t_seq = ev[1].elapsed_time(ev[2]) / 1e3
+    # One ckr_render call per job through the public entry point (a scene per
+    # material set; the second of two passes is timed).
+    scenes = [S.RenderScene(S.SceneData(sd.tri9, sd.tri_mat, sd.sph4, sd.sph_mat,
+                                        [S.Material.from_buffer_copy(mats[j * sd.nmat + k]) for k in range(sd.nmat)],
+                                        [sd.lights[k] for k in range(sd.nlights)])) for j in range(len(params))]
+    cfgs = [S.render_cfg(shader=S.SHADER_PATH, spp=p["spp"], max_depth=p["max_depth"], n_light=1, n_brdf=1,
+                         rr_prob=0.3, seed=p["seed"]) for p in params]
+    for rep in range(2):
+        ev[2].record(s)
+        for sc, p, c, o in zip(scenes, params, cfgs, outs):
+            sc.render(p["cam"], c, o.data_ptr(), None, s.cuda_stream)
+        ev[3].record(s)
+        torch.cuda.synchronize()
+    t_api = ev[2].elapsed_time(ev[3]) / 1e3
+    return {"workload": "64 box-scene jobs, random sphere BRDFs and yaw, 256^2..1024^2, 4/16/64 spp, depth 3/6, "
+                        "path tracer with MIS",
+            "samples": paths, "graph_launches": launches,
+            "batched_graph": {"sec": round(t_graph, 4), "samples_per_s": round(paths / t_graph, 1)},
+            "sequential_per_job": {"sec": round(t_seq, 4), "samples_per_s": round(paths / t_seq, 1)},
+            "one_ckr_render_per_job": {"sec": round(t_api, 4), "samples_per_s": round(paths / t_api, 1)},
+            "speedup": round(t_seq / t_graph, 3),
+            "speedup_vs_ckr_render_per_job": round(t_api / t_graph, 3),
+            "autotuner": {"block": tune.block, "wave": tune.wave, "candidates": tune.candidates,
+                          "reduced_batch_ms": round(tune.ms, 3)},
+            "create_and_capture_s": round(create_s, 2)}
+
+
 def cpu_side_baselines(tri_unused=None):
     """FP64 restatements of the reference on the host cores for the box render
     (path tracer, 64x64 x 16 spp sample) and LTC shading (65,536 pixels)."""
@@ -511,6 +570,7 @@ def main():
     line["box_render"] = bench_box_render(torch, args.steps)
     line["ltc_shade"] = bench_ltc(torch, args.steps)
     line["manylight"] = bench_manylight(torch)
+    line["batch"] = bench_batch(torch)
     if not args.no_cpu_baseline:
         cb, ref_counts = cpu_baseline(tri, closest)
         line["cpu_baseline"] = cb

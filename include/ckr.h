@@ -236,6 +236,49 @@ int ckr_render(ckr_scene *scene, const ckr_camera *cam, const ckr_render_cfg *cf
 int ckr_render_noalloc(ckr_scene *scene, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb,
                        void *stream);
 
+/* ---- batched rendering (no reference counterpart) -------------------------
+ * Many jobs of uneven resolution, spp and depth over one scene's geometry are
+ * rendered by one wavefront pass: their paths are numbered consecutively and
+ * packed into shared waves, so the GPU stays full across job boundaries.  The
+ * whole pass (every wave, bounce and resolve) is a fixed launch sequence with no
+ * host synchronisation; it is captured once into a CUDA graph and replayed.
+ * Each job may use its own material table (same layout as the scene's, e.g.
+ * other sphere BRDFs).  Block size and wave size come from an autotuner that
+ * times candidates on a reduced copy of the batch (spp capped at 1). */
+typedef struct ckr_job {
+  ckr_camera cam;        /* resolution: cam.width x cam.height */
+  uint32_t spp, max_depth;
+  uint64_t seed;         /* per-pixel stream key = hash(seed, pixel) as in ckr_render */
+  uint32_t material_set; /* index of the batch material table the job uses */
+  uint32_t reserved;
+  float *rgb;            /* device output, width x height x 3 floats, top row first */
+} ckr_job;
+
+typedef struct ckr_batch_tuning {
+  uint32_t block;  /* threads per block of the wavefront kernels: 64, 128 or 256 */
+  uint32_t wave;   /* paths per wave (queue capacity), >= 1024 */
+  float ms;        /* autotuner: time of the reduced batch with these values */
+  uint32_t candidates; /* autotuner: configurations timed */
+} ckr_batch_tuning;
+
+typedef struct ckr_batch ckr_batch;
+/* shader: CKR_SHADER_PATH (n_light_samples per light, one BRDF sample) or
+ * CKR_SHADER_PATH_NEE; rr_prob as in ckr_render_cfg.  materials: nsets tables of
+ * the scene's material count each (NULL, 0: the scene's own, set 0).  tuning NULL:
+ * autotune.  Jobs' rgb buffers are recorded in the graph: keep them alive. */
+int ckr_batch_create(ckr_scene *scene, uint32_t shader, float rr_prob, uint32_t n_light_samples,
+                     const ckr_material *materials, uint32_t nsets, const ckr_job *jobs, uint32_t njobs,
+                     const ckr_batch_tuning *tuning, ckr_batch **out);
+/* One replay of the captured graph on `stream` (asynchronous). */
+int ckr_batch_render(ckr_batch *batch, void *stream);
+/* The same jobs one after another, each with its own waves and launches (no
+ * packing across jobs, no graph): the baseline the batch is measured against. */
+int ckr_batch_render_sequential(ckr_batch *batch, void *stream);
+int ckr_batch_get_tuning(const ckr_batch *batch, ckr_batch_tuning *out);
+/* Paths (samples) per replay and launches in the captured graph. */
+int ckr_batch_get_stats(const ckr_batch *batch, uint64_t *paths, uint32_t *launches);
+int ckr_batch_destroy(ckr_batch *batch);
+
 /* ---- learned light selection (no reference counterpart) -------------------
  * A proposal is a small network that maps a shading point (position, normal,
  * outgoing direction, GGX roughness) to a distribution over the scene's emitter

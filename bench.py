@@ -434,6 +434,51 @@ def cpu_side_baselines(tri_unused=None):
             "kind": "port"}
 
 
+def case_manylight_learned():
+    """Small case of the many-light workload for profilers: 640x360, 16 spp, depth 6,
+    one learned render training for 40 Adam steps (minibatch 16384)."""
+    import torch
+    from chakumrender_gb300 import build
+    from chakumrender_gb300 import scene as S
+    from chakumrender_gb300.proposal import Proposal
+
+    build.build_library()
+    sd = S.manylight_scene(S.manylight_spec(width=640, height=360))
+    scene = S.RenderScene(sd)
+    rgb = torch.empty((360, 640, 3), dtype=torch.float32, device="cuda")
+    prop = Proposal(scene, seed=1, minibatch=16384, max_steps=40)
+    prop.render(sd.camera, S.render_cfg(shader=S.SHADER_PATH_NEE, spp=16, max_depth=6, seed=10), rgb.data_ptr())
+    torch.cuda.synchronize()
+    st = prop.status()[0]
+    if st != 0:
+        raise SystemExit(f"proposal error {st}")
+
+
+def case_manylight_split():
+    """One frozen learned render and one plain render of the many-light workload at
+    640x360, 16 spp, depth 6 (after a 200-step training render), for launch lists."""
+    import torch
+    from chakumrender_gb300 import build
+    from chakumrender_gb300 import scene as S
+    from chakumrender_gb300.proposal import Proposal
+
+    build.build_library()
+    sd = S.manylight_scene(S.manylight_spec(width=640, height=360))
+    scene = S.RenderScene(sd)
+    cam = sd.camera
+    rgb = torch.empty((360, 640, 3), dtype=torch.float32, device="cuda")
+    prop = Proposal(scene, seed=1, minibatch=16384, max_steps=200)
+    cfg = lambda seed: S.render_cfg(shader=S.SHADER_PATH_NEE, spp=16, max_depth=6, seed=seed)
+    prop.render(cam, cfg(10), rgb.data_ptr())
+    prop.set_training(False)
+    prop.render(cam, cfg(11), rgb.data_ptr())
+    scene.render(cam, cfg(1), rgb.data_ptr())
+    torch.cuda.synchronize()
+
+
+CASES = {"manylight-learned": case_manylight_learned, "manylight-split": case_manylight_split}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -442,7 +487,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--leaf", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--case", default=None, choices=sorted(CASES),
+                    help="run one small workload and exit (for profiling; prints nothing to parse)")
     args = ap.parse_args()
+    if args.case:
+        return CASES[args.case]()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

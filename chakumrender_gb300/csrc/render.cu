@@ -32,6 +32,12 @@ namespace {
 
 constexpr int kRTPB = 128;  // block size of the single-render kernels
 
+uint32_t mesh_lights_of(const ckr_scene *s) {
+  uint32_t n = 0;
+  for (const DevLight &L : s->host_lights) n += L.type == CKR_LIGHT_MESH;
+  return n;
+}
+
 struct Workspace {
   DevBuf<float4> ray_o, ray_d, beta, sh_o, sh_d, sh_c;
   DevBuf<uint4> meta;
@@ -56,7 +62,7 @@ namespace {
 
 int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb,
                 double *accum, void *stream_) {
-  if (!s || !cam || !cfg || !rgb || cam->width == 0 || cam->height == 0 || cfg->spp == 0 || cfg->shader > 3)
+  if (!s || !cam || !cfg || !rgb || cam->width == 0 || cam->height == 0 || cfg->spp == 0 || cfg->shader > 4)
     return CKR_ERR_INVALID_ARGUMENT;
   if (!s->has_shading) return CKR_ERR_INVALID_ARGUMENT;
   if (cfg->max_depth > 60 || cfg->spp > 65536 || cfg->n_light_samples > 256 || cfg->n_brdf_samples > 256)
@@ -86,6 +92,7 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   uint32_t per_path = cfg->shader == CKR_SHADER_PATH_NEE
                           ? 1u
                           : point_lights + area_lights * prm.n_light + (cfg->shader == CKR_SHADER_DIRECT_MIS ? prm.n_brdf : 0);
+  if (cfg->shader == CKR_SHADER_DIRECT_CV) per_path = mesh_lights_of(s) * prm.n_light;
   prm.shadow_per_path = std::max(1u, per_path);
   uint64_t total = (uint64_t)prm.npix * prm.spp;
   size_t wave = (size_t)std::min<uint64_t>(total, std::max<uint64_t>(32768, (1ull << 23) / prm.shadow_per_path));
@@ -156,6 +163,7 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   const int g_sh = grid_for((const void *)k_shadow<kRTPB>, smem, kRTPB);
   const void *shade_fn = cfg->shader == CKR_SHADER_PATH_NEE ? (const void *)k_shade_nee<kRTPB>
                          : cfg->shader == CKR_SHADER_PATH      ? (const void *)k_shade<CKR_SHADER_PATH, kRTPB>
+                         : cfg->shader == CKR_SHADER_DIRECT_CV  ? (const void *)k_shade<CKR_SHADER_DIRECT_CV, kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_MIS ? (const void *)k_shade<CKR_SHADER_DIRECT_MIS, kRTPB>
                                                                 : (const void *)k_shade<CKR_SHADER_DIRECT_MISCV, kRTPB>;
   const int g_shade = grid_for(shade_fn, 0, kRTPB);
@@ -193,6 +201,8 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
         k_shade_nee<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, lr);
       else if (cfg->shader == CKR_SHADER_PATH)
         k_shade<CKR_SHADER_PATH, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
+      else if (cfg->shader == CKR_SHADER_DIRECT_CV)
+        k_shade<CKR_SHADER_DIRECT_CV, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else if (cfg->shader == CKR_SHADER_DIRECT_MIS)
         k_shade<CKR_SHADER_DIRECT_MIS, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else
@@ -320,7 +330,7 @@ int noalloc_setup(int dev) {
 
 extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb,
                                   void *stream_) {
-  if (!s || !cam || !cfg || !rgb || cam->width == 0 || cam->height == 0 || cfg->spp == 0 || cfg->shader > 3)
+  if (!s || !cam || !cfg || !rgb || cam->width == 0 || cam->height == 0 || cfg->spp == 0 || cfg->shader > 4)
     return CKR_ERR_INVALID_ARGUMENT;
   if (!s->has_shading) return CKR_ERR_INVALID_ARGUMENT;
   if (cfg->max_depth > 60 || cfg->spp > 65536 || cfg->n_light_samples > 256 || cfg->n_brdf_samples > 256)
@@ -349,6 +359,7 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
                           ? 1u
                           : (uint64_t)point_lights + (uint64_t)area_lights * prm.n_light +
                                 (cfg->shader == CKR_SHADER_DIRECT_MIS ? prm.n_brdf : 0);
+  if (cfg->shader == CKR_SHADER_DIRECT_CV) per_path = (uint64_t)mesh_lights_of(s) * prm.n_light;
   if (per_path > kNoAllocShadow) return CKR_ERR_TOO_LARGE;
   prm.shadow_per_path = (uint32_t)std::max<uint64_t>(1, per_path);
   uint64_t total = (uint64_t)prm.npix * prm.spp;
@@ -400,6 +411,7 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
   const int g_sh = grid_for((const void *)k_shadow<kRTPB>, smem, kRTPB);
   const void *shade_fn = cfg->shader == CKR_SHADER_PATH_NEE ? (const void *)k_shade_nee<kRTPB>
                          : cfg->shader == CKR_SHADER_PATH      ? (const void *)k_shade<CKR_SHADER_PATH, kRTPB>
+                         : cfg->shader == CKR_SHADER_DIRECT_CV  ? (const void *)k_shade<CKR_SHADER_DIRECT_CV, kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_MIS ? (const void *)k_shade<CKR_SHADER_DIRECT_MIS, kRTPB>
                                                                 : (const void *)k_shade<CKR_SHADER_DIRECT_MISCV, kRTPB>;
   const int g_shade = grid_for(shade_fn, 0, kRTPB);
@@ -415,6 +427,8 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
         k_shade_nee<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, Learn{});
       else if (cfg->shader == CKR_SHADER_PATH)
         k_shade<CKR_SHADER_PATH, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
+      else if (cfg->shader == CKR_SHADER_DIRECT_CV)
+        k_shade<CKR_SHADER_DIRECT_CV, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else if (cfg->shader == CKR_SHADER_DIRECT_MIS)
         k_shade<CKR_SHADER_DIRECT_MIS, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else

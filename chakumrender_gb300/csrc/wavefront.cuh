@@ -297,6 +297,84 @@ __device__ uint32_t light_samples(const ShadeView &sv, const Params &prm, const 
   return cnt;
 }
 
+// getLightAnalytic / getLightAnalyticDiffuse over every mesh light
+// (src/lightSources_CV.cpp:221-321): spec * amplitude * sum L |I_ltc| / 2pi +
+// (1 - spec) * sum L |I_cos| / 2pi.
+__device__ __forceinline__ F3 ltc_term(const ShadeView &sv, const Surface &S, const Material &M, const LtcLookup &Lk,
+                                       const M3f &minv, bool ltc_on) {
+  F3 G = f3(0, 0, 0);
+  for (uint32_t k = 0; k < sv.nlights; ++k) {
+    DevLight L = sv.lights[k];
+    if (L.type != CKR_LIGHT_MESH) continue;
+    F3 gs = f3(0, 0, 0), gd = f3(0, 0, 0);
+    for (uint32_t j = 0; j < L.count; ++j) {
+      const float *t9 = sv.tri9 + 9 * (size_t)(L.first + j);
+      F3 A = f3(t9[0], t9[1], t9[2]), B = f3(t9[3], t9[4], t9[5]), C = f3(t9[6], t9[7], t9[8]);
+      F3 Le = mat_radiance(sv, sv.tri_mat[L.first + j]);
+      float s = ltc_on ? ltc_spec_tri(A, B, C, S.x, minv) : 0.f;
+      float d = ltc_diffuse_tri(A, B, C, S.n, S.x);
+      gs = gs + Le * s;
+      gd = gd + Le * d;
+    }
+    const float inv2pi = 1.0f / (2.0f * kPi);
+    G = G + gs * (inv2pi * (ltc_on ? Lk.amp : 0.f) * M.spec) + gd * (inv2pi * (1.0f - M.spec));
+  }
+  return G;
+}
+
+// The sampled part of getLightFromMeshSource_AnalyticCV (src/lightSources_CV.cpp:335-397):
+// per mesh light, n_light points by MeshLight::getSamples (300-bin CDF, sqrt(u1)
+// barycentrics), each adding Le (V f - f_ltc) cos cos_l / d^2 * area / n.  The
+// unoccluded -f_ltc part is summed into `neg`; each +f part is a shadow ray whose
+// contribution is returned through so/sd/sc when WRITE.  Returns the ray count.
+template <bool WRITE>
+__device__ uint32_t cv_samples(const ShadeView &sv, const Params &prm, const Surface &S, const Material &M, float refl,
+                               const LtcLookup &Lk, const M3f &minv, bool ltc_on, F3 col, uint64_t key,
+                               uint32_t sample, F3 o_off, F3 &neg, float4 *so, float4 *sd, float4 *sc) {
+  uint32_t cnt = 0, sidx = 0;
+  for (uint32_t k = 0; k < sv.first_point; ++k) {
+    DevLight L = sv.lights[k];
+    if (L.type != CKR_LIGHT_MESH) continue;
+    const float w_area = L.area / (float)prm.n_light;
+    for (uint32_t i = 0; i < prm.n_light; ++i, ++sidx) {
+      float e0 = ckr_draw_f(key, ctr(sample, 0, 3 * sidx));
+      float e1 = ckr_draw_f(key, ctr(sample, 0, 3 * sidx + 1));
+      float e2 = ckr_draw_f(key, ctr(sample, 0, 3 * sidx + 2));
+      uint32_t b = (uint32_t)(e0 * (float)kInvCdfBins);
+      b = b >= kInvCdfBins ? kInvCdfBins - 1 : b;
+      const uint32_t tri = L.first + __ldg(&sv.cdf[L.cdf + b]);
+      const float *t9 = sv.tri9 + 9 * (size_t)tri;
+      F3 A = f3(__ldg(t9), __ldg(t9 + 1), __ldg(t9 + 2));
+      F3 B = f3(__ldg(t9 + 3), __ldg(t9 + 4), __ldg(t9 + 5));
+      F3 C = f3(__ldg(t9 + 6), __ldg(t9 + 7), __ldg(t9 + 8));
+      F3 Pl = sample_triangle(A, B, C, e1, e2);
+      F3 dv = Pl - S.x;
+      float d2 = dot(dv, dv), d = sqrtf(d2);
+      F3 w = dv * (1.0f / d);
+      float c = dot(w, S.n);
+      if (c < 0.f) continue;
+      float c1 = fabsf(dot(w, tri_normal(sv, tri)));
+      float g = c * c1 / d2 * w_area;
+      F3 Le = mat_radiance(sv, sv.tri_mat[tri]);
+      float fa = brdf_eval(M, S.n, S.wo_ref, S.wo, w) * refl;
+      if (!WRITE) {
+        float fl = (ltc_on ? brdf_ltc(M, Lk, minv, S.n, w) : brdf_eval(M, S.n, S.wo_ref, S.wo, w)) * refl;
+        neg = neg - Le * (fl * g);
+      }
+      if (fa > 0.f) {
+        if (WRITE) {
+          F3 contrib = mulc(col, Le) * (fa * g);
+          so[cnt] = make_float4(o_off.x, o_off.y, o_off.z, 0.f);
+          sd[cnt] = make_float4(w.x, w.y, w.z, shadow_tmax(length(Pl - o_off)));
+          sc[cnt] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
+        }
+        ++cnt;
+      }
+    }
+  }
+  return cnt;
+}
+
 template <uint32_t SHADER, int TPB>
 __global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params prm, int cur, int depth,
                                                  const LtcEntry *__restrict__ ltc) {
@@ -358,39 +436,47 @@ __global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params pr
       }
     }
     // ---- direct light: count the shadow rays, reserve, then write them ----
-    if (surface && SHADER != CKR_SHADER_DIRECT_MISCV)
+    LtcLookup Lk{};
+    M3f minv{};
+    bool ltc_on = false;
+    F3 cv_neg = f3(0, 0, 0);
+    if (surface && (SHADER == CKR_SHADER_DIRECT_MISCV || SHADER == CKR_SHADER_DIRECT_CV)) {
+      auto tab = [&](int idx) { return ltc[idx]; };
+      float theta = acosf(fminf(1.0f, fmaxf(-1.0f, dot(S.n, S.wo))));
+      Lk = ltc_lookup(tab, theta, M.alpha);
+      minv = ltc_minv_world(Lk, S.n, S.wo);
+      ltc_on = M.brdf == kGGX || M.brdf == kGGXApprox;
+    }
+    if (surface && SHADER == CKR_SHADER_DIRECT_CV)
+      nshadow = cv_samples<false>(sv, prm, S, M, sv.mats[S.mat].reflectance, Lk, minv, ltc_on,
+                                  f3(sv.mats[S.mat].color[0], sv.mats[S.mat].color[1], sv.mats[S.mat].color[2]), key,
+                                  meta.y, o_off, cv_neg, nullptr, nullptr, nullptr);
+    else if (surface && SHADER != CKR_SHADER_DIRECT_MISCV)
       nshadow = light_samples<SHADER == CKR_SHADER_DIRECT_MIS>(sv, prm, S, M, fcol, beta, key, meta.y, meta.z, o_off,
                                                                nullptr, nullptr, nullptr, false);
     uint32_t sbase = warp_reserve(&P.counts[2], nshadow);
     if (nshadow) {
-      light_samples<SHADER == CKR_SHADER_DIRECT_MIS>(sv, prm, S, M, fcol, beta, key, meta.y, meta.z, o_off,
-                                                     P.sh_o + sbase, P.sh_d + sbase, P.sh_c + sbase, true);
+      if (SHADER == CKR_SHADER_DIRECT_CV) {
+        F3 unused = f3(0, 0, 0);
+        cv_samples<true>(sv, prm, S, M, sv.mats[S.mat].reflectance, Lk, minv, ltc_on,
+                         f3(sv.mats[S.mat].color[0], sv.mats[S.mat].color[1], sv.mats[S.mat].color[2]), key, meta.y,
+                         o_off, unused, P.sh_o + sbase, P.sh_d + sbase, P.sh_c + sbase);
+      } else {
+        light_samples<SHADER == CKR_SHADER_DIRECT_MIS>(sv, prm, S, M, fcol, beta, key, meta.y, meta.z, o_off,
+                                                       P.sh_o + sbase, P.sh_d + sbase, P.sh_c + sbase, true);
+      }
       for (uint32_t k = 0; k < nshadow; ++k) P.sh_px[sbase + k] = meta.x;
+    }
+    if (surface && SHADER == CKR_SHADER_DIRECT_CV) {
+      // getLightFromMeshSource_AnalyticCV: the LTC term plus the unoccluded part of
+      // the sampled residual; the occluded part arrives through the shadow rays.
+      const ckr_material &mm = sv.mats[S.mat];
+      F3 col = f3(mm.color[0], mm.color[1], mm.color[2]);
+      add_px(P.accum, meta.x, mulc(col, ltc_term(sv, S, M, Lk, minv, ltc_on) + cv_neg));
     }
     if (surface && SHADER == CKR_SHADER_DIRECT_MISCV) {
       // getLightFromMeshSource_Analytic_MISCV (src/lightSources_CV.cpp:399-450).
-      auto tab = [&](int idx) { return ltc[idx]; };
-      float theta = acosf(fminf(1.0f, fmaxf(-1.0f, dot(S.n, S.wo))));
-      LtcLookup Lk = ltc_lookup(tab, theta, M.alpha);
-      M3f minv = ltc_minv_world(Lk, S.n, S.wo);
-      bool ltc_on = M.brdf == kGGX || M.brdf == kGGXApprox;
-      F3 G = f3(0, 0, 0);
-      for (uint32_t k = 0; k < sv.nlights; ++k) {
-        DevLight L = sv.lights[k];
-        if (L.type != CKR_LIGHT_MESH) continue;
-        F3 gs = f3(0, 0, 0), gd = f3(0, 0, 0);
-        for (uint32_t j = 0; j < L.count; ++j) {
-          const float *t9 = sv.tri9 + 9 * (size_t)(L.first + j);
-          F3 A = f3(t9[0], t9[1], t9[2]), B = f3(t9[3], t9[4], t9[5]), C = f3(t9[6], t9[7], t9[8]);
-          F3 Le = mat_radiance(sv, sv.tri_mat[L.first + j]);
-          float s = ltc_on ? ltc_spec_tri(A, B, C, S.x, minv) : 0.f;
-          float d = ltc_diffuse_tri(A, B, C, S.n, S.x);
-          gs = gs + Le * s;
-          gd = gd + Le * d;
-        }
-        const float inv2pi = 1.0f / (2.0f * kPi);
-        G = G + gs * (inv2pi * (ltc_on ? Lk.amp : 0.f) * M.spec) + gd * (inv2pi * (1.0f - M.spec));
-      }
+      F3 G = ltc_term(sv, S, M, Lk, minv, ltc_on);
       // MIS residual over the getSamples set; visibility is 1 in the reference.
       F3 res = f3(0, 0, 0);
       const uint32_t nb = prm.n_brdf, nlobe = (uint32_t)((float)nb * M.spec);

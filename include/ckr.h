@@ -198,6 +198,11 @@ typedef struct ckr_camera {
  * heuristic between the two; Russian roulette with rr_prob.  ckr_render selects
  * lights in proportion to power; ckr_render_learned with a proposal network. */
 #define CKR_SHADER_PATH_NEE 3
+/* shadeDirectOnly + getLightFromMeshSource_AnalyticCV (src/lightSources_CV.cpp:335-397):
+ * the LTC analytic term plus a control-variate residual over n_light_samples area
+ * samples per mesh light, sum Le (V f - f_ltc) cos cos_l / d^2 * area / n, with
+ * shadow rays for V. */
+#define CKR_SHADER_DIRECT_CV 4
 
 typedef struct ckr_render_cfg {
   uint32_t shader;           /* CKR_SHADER_* */

@@ -22,6 +22,7 @@ CASES = [
     (S.SHADER_DIRECT_MISCV, 4, 10, 60, 1, 1e-4),
     (S.SHADER_DIRECT_MIS, 4, 10, 60, 1, 1e-4),
     (S.SHADER_PATH, 16, 1, 1, 4, 1e-3),
+    (S.SHADER_DIRECT_CV, 4, 25, 0, 1, 1e-4),
 ]
 
 
@@ -38,17 +39,19 @@ def test_box_vs_oracle(torch_cuda, shader, spp, nl, nb, depth, bar):
     cfg = S.render_cfg(shader=shader, spp=spp, n_light=nl, n_brdf=nb, max_depth=depth)
     g = gpu_render(torch_cuda, sd, sd.camera, cfg)
     o = O.render(sd, sd.camera, cfg)
-    assert np.all(np.isfinite(g)) and g.min() >= 0
+    # The control-variate estimator may dip below zero per pixel (V f - f_ltc < 0).
+    assert np.all(np.isfinite(g)) and (g.min() >= 0 or shader == S.SHADER_DIRECT_CV)
     e = rel_mse(g, o)
     print(f"shader {shader}: relMSE vs oracle {e:.3e}, mean {g.mean():.5f} vs {o.mean():.5f}")
     assert e <= bar
     assert abs(g.mean() - o.mean()) <= 1e-3 * o.mean() + 1e-6
 
 
-@pytest.mark.parametrize("name,shader", [("scene0", S.SHADER_DIRECT_MISCV), ("scene1", S.SHADER_DIRECT_MIS)])
+@pytest.mark.parametrize("name,shader", [("scene0", S.SHADER_DIRECT_MISCV), ("scene1", S.SHADER_DIRECT_MIS),
+                                         ("scene0", S.SHADER_DIRECT_CV)])
 def test_reference_scenes_vs_oracle(torch_cuda, name, shader):
     sd = from_arrays(np.load(GOLD / "ref_scenes.npz"), name)
-    cfg = S.render_cfg(shader=shader, spp=1, n_light=10, n_brdf=60)
+    cfg = S.render_cfg(shader=shader, spp=1, n_light=25 if shader == S.SHADER_DIRECT_CV else 10, n_brdf=60)
     g = gpu_render(torch_cuda, sd, sd.camera, cfg)
     o = O.render(sd, sd.camera, cfg)
     e = rel_mse(g, o)

@@ -122,3 +122,24 @@ def test_xml_errors(tmp_path):
     assert L.ckr_xml_load(str(bad).encode(), C.byref(h)) == -8
     bad.write_text("<SCREEN><WIDTH>4</WIDTH><HEIGHT>4")
     assert L.ckr_xml_load(str(bad).encode(), C.byref(h)) == -8
+
+
+def test_oracle_cv_shader_is_ltc_term_where_unoccluded():
+    """getLightFromMeshSource_AnalyticCV on Lambertian surfaces: where no sample is
+    occluded the residual V f - f_ltc vanishes sample by sample, so the estimate is
+    the LTC term exactly (zero variance across seeds); where the sphere shadows the
+    floor it is lower."""
+    import oracle as O
+
+    sd = S.load_xml(S.SCENES / "box.xml")
+    mats = [S.Material.from_buffer_copy(sd.materials[i]) for i in range(sd.nmat)]
+    for k in (10, 11):
+        mats[k].brdf, mats[k].spec, mats[k].alpha = 2, 0.0, 0.5
+    d = S.SceneData(sd.tri9, sd.tri_mat, sd.sph4, sd.sph_mat, mats, [sd.lights[i] for i in range(sd.nlights)])
+    cam = sd.camera
+    cam.width = cam.height = 24
+    a = O.render(d, cam, S.render_cfg(shader=S.SHADER_DIRECT_CV, spp=16, n_light=8, n_brdf=0, seed=1))
+    b = O.render(d, cam, S.render_cfg(shader=S.SHADER_DIRECT_CV, spp=16, n_light=8, n_brdf=0, seed=2))
+    same = np.all(np.abs(a - b) < 1e-12, axis=2)
+    assert 0.5 < same.mean() < 1.0  # most pixels unshadowed, some in the spheres' shadows
+    assert np.all(np.isfinite(a))

@@ -62,7 +62,7 @@ namespace {
 
 int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb,
                 double *accum, void *stream_) {
-  if (!s || !cam || !cfg || !rgb || cam->width == 0 || cam->height == 0 || cfg->spp == 0 || cfg->shader > 4)
+  if (!s || !cam || !cfg || !rgb || cam->width == 0 || cam->height == 0 || cfg->spp == 0 || cfg->shader > 5)
     return CKR_ERR_INVALID_ARGUMENT;
   if (!s->has_shading) return CKR_ERR_INVALID_ARGUMENT;
   if (cfg->max_depth > 60 || cfg->spp > 65536 || cfg->n_light_samples > 256 || cfg->n_brdf_samples > 256)
@@ -79,11 +79,12 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   Params prm{};
   prm.shader = cfg->shader;
   prm.spp = cfg->spp;
-  const bool path = cfg->shader == CKR_SHADER_PATH || cfg->shader == CKR_SHADER_PATH_NEE;
+  const bool path = cfg->shader == CKR_SHADER_PATH || cfg->shader == CKR_SHADER_PATH_NEE ||
+                    cfg->shader == CKR_SHADER_EXPLICIT;
   if (cfg->shader == CKR_SHADER_PATH_NEE && s->n_emit == 0) return CKR_ERR_INVALID_ARGUMENT;
   prm.max_depth = path ? std::max(1u, cfg->max_depth) : 1u;
   prm.n_light = cfg->n_light_samples;
-  prm.n_brdf = path ? 1u : cfg->n_brdf_samples;
+  prm.n_brdf = path && cfg->shader != CKR_SHADER_EXPLICIT ? 1u : cfg->n_brdf_samples;
   prm.rr_prob = path ? cfg->rr_prob : 0.f;
   prm.seed = cfg->seed;
   prm.npix = cam->width * cam->height;
@@ -93,6 +94,7 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
                           ? 1u
                           : point_lights + area_lights * prm.n_light + (cfg->shader == CKR_SHADER_DIRECT_MIS ? prm.n_brdf : 0);
   if (cfg->shader == CKR_SHADER_DIRECT_CV) per_path = mesh_lights_of(s) * prm.n_light;
+  if (cfg->shader == CKR_SHADER_EXPLICIT) per_path = 0;  // the MISCV direct term traces no shadow rays
   prm.shadow_per_path = std::max(1u, per_path);
   uint64_t total = (uint64_t)prm.npix * prm.spp;
   size_t wave = (size_t)std::min<uint64_t>(total, std::max<uint64_t>(32768, (1ull << 23) / prm.shadow_per_path));
@@ -161,12 +163,16 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   }
   const int g_ext = grid_for((const void *)k_extend<kRTPB>, smem, kRTPB);
   const int g_sh = grid_for((const void *)k_shadow<kRTPB>, smem, kRTPB);
-  const void *shade_fn = cfg->shader == CKR_SHADER_PATH_NEE ? (const void *)k_shade_nee<kRTPB>
+  if (cfg->shader == CKR_SHADER_EXPLICIT && smem > 48 * 1024)
+    CKR_CUDA_TRY(cudaFuncSetAttribute(k_shade<CKR_SHADER_EXPLICIT, kRTPB>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const void *shade_fn = cfg->shader == CKR_SHADER_EXPLICIT ? (const void *)k_shade<CKR_SHADER_EXPLICIT, kRTPB>
+                         : cfg->shader == CKR_SHADER_PATH_NEE ? (const void *)k_shade_nee<kRTPB>
                          : cfg->shader == CKR_SHADER_PATH      ? (const void *)k_shade<CKR_SHADER_PATH, kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_CV  ? (const void *)k_shade<CKR_SHADER_DIRECT_CV, kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_MIS ? (const void *)k_shade<CKR_SHADER_DIRECT_MIS, kRTPB>
                                                                 : (const void *)k_shade<CKR_SHADER_DIRECT_MISCV, kRTPB>;
-  const int g_shade = grid_for(shade_fn, 0, kRTPB);
+  const int g_shade = grid_for(shade_fn, cfg->shader == CKR_SHADER_EXPLICIT ? smem : 0, kRTPB);
   for (uint64_t base = 0; base < total; base += wave) {
     uint32_t n = (uint32_t)std::min<uint64_t>(wave, total - base);
     k_camera<kRTPB><<<std::min<int>(g_ext, ceil_div(n, kRTPB)), kRTPB, 0, stream>>>(c, P, prm, base, n);
@@ -197,7 +203,9 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
           lr.rec_cap = prop->batch;
         }
       }
-      if (cfg->shader == CKR_SHADER_PATH_NEE)
+      if (cfg->shader == CKR_SHADER_EXPLICIT)
+        k_shade<CKR_SHADER_EXPLICIT, kRTPB><<<g_shade, kRTPB, smem, stream>>>(shv, P, prm, cur, (int)d, ltc, sv, depth);
+      else if (cfg->shader == CKR_SHADER_PATH_NEE)
         k_shade_nee<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, lr);
       else if (cfg->shader == CKR_SHADER_PATH)
         k_shade<CKR_SHADER_PATH, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);

@@ -31,6 +31,17 @@ __device__ __forceinline__ F3 offset_origin(F3 p, F3 n) {
 // slack t + 1e-5 < d (src/shader.cpp:84-92), made relative for FP32 at large d.
 __device__ __forceinline__ float shadow_tmax(float d) { return d - 1e-5f * fmaxf(1.0f, d); }
 
+// Shadow ray from the offset origin o to the light point p: direction and tmax.  The
+// ray must aim from o itself: aimed along the direction from the unoffset surface
+// point, it meets the light's plane up to |offset| (1/cos - cos) before p, which
+// exceeds the slack at moderate angles, and the light would occlude itself.
+__device__ __forceinline__ float4 shadow_dir(F3 o, F3 p) {
+  F3 v = p - o;
+  float l = length(v);
+  v = v * (1.0f / l);
+  return make_float4(v.x, v.y, v.z, shadow_tmax(l));
+}
+
 struct Surface {
   F3 x, n, wo, wo_ref;
   uint32_t mat;

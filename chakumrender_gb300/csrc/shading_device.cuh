@@ -189,6 +189,17 @@ SHD F3 sample_cosine(F3 n, float e1, float e2) {
   return to_world(X, Y, n, st * cp, st * sp, ct);
 }
 
+// Uniform direction on the hemisphere about n (getHemiDirectionSamples,
+// src/domainSampler.cpp:89-100: a uniform sphere direction turned into n's
+// hemisphere; 1/pdf = 2 pi).
+SHD F3 sample_hemisphere(F3 n, float e1, float e2) {
+  F3 X, Y;
+  ref_frame(n, X, Y);
+  float ct = e1, st = sqrtf(fmaxf(0.0f, 1.0f - e1 * e1)), sp, cp;
+  sincosf(2.0f * kPi * e2, &sp, &cp);
+  return to_world(X, Y, n, st * cp, st * sp, ct);
+}
+
 // Specular lobe of getBrdfDirectionSamples / getClassicPhongDirectionSamples
 // (src/domainSampler.cpp:193-314).
 SHD F3 sample_lobe(const Material &m, F3 n, F3 wo_ref, F3 wo, float e1, float e2) {

@@ -187,6 +187,7 @@ __global__ void __launch_bounds__(TPB) k_extend(SceneView s, Paths P, int cur, i
   for (uint32_t i = blockIdx.x * TPB + threadIdx.x; i < n; i += gridDim.x * TPB) {
     uint32_t slot = q[i];
     float4 a = P.ray_o[slot], b = P.ray_d[slot];
+    if (a.w < 0.f) continue;  // traced by the shading kernel (CKR_SHADER_EXPLICIT)
     RayPre r = make_ray(a, b);
     float t = b.w;
     uint32_t id = trace_ray<false>(s, r, t, stack, TPB, depth);
@@ -365,7 +366,7 @@ __device__ uint32_t cv_samples(const ShadeView &sv, const Params &prm, const Sur
         if (WRITE) {
           F3 contrib = mulc(col, Le) * (fa * g);
           so[cnt] = make_float4(o_off.x, o_off.y, o_off.z, 0.f);
-          sd[cnt] = make_float4(w.x, w.y, w.z, shadow_tmax(length(Pl - o_off)));
+          sd[cnt] = shadow_dir(o_off, Pl);
           sc[cnt] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
         }
         ++cnt;
@@ -375,9 +376,14 @@ __device__ uint32_t cv_samples(const ShadeView &sv, const Params &prm, const Sur
   return cnt;
 }
 
+// Continuation dims of CKR_SHADER_EXPLICIT: RR at kDimRR, redraws r < kExplicitTries
+// of the hemisphere direction at kDimHemi + 2r, + 2r + 1.
+constexpr uint32_t kDimHemi = 1004, kExplicitTries = 8;
+
 template <uint32_t SHADER, int TPB>
 __global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params prm, int cur, int depth,
-                                                 const LtcEntry *__restrict__ ltc) {
+                                                 const LtcEntry *__restrict__ ltc, SceneView scene = SceneView{},
+                                                 int stack_depth = 0) {
   const uint32_t n = P.counts[cur];
   const uint32_t *q = cur ? P.q1 : P.q0;
   uint32_t *qn = cur ? P.q0 : P.q1;
@@ -440,7 +446,8 @@ __global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params pr
     M3f minv{};
     bool ltc_on = false;
     F3 cv_neg = f3(0, 0, 0);
-    if (surface && (SHADER == CKR_SHADER_DIRECT_MISCV || SHADER == CKR_SHADER_DIRECT_CV)) {
+    if (surface && (SHADER == CKR_SHADER_DIRECT_MISCV || SHADER == CKR_SHADER_DIRECT_CV ||
+                    SHADER == CKR_SHADER_EXPLICIT)) {
       auto tab = [&](int idx) { return ltc[idx]; };
       float theta = acosf(fminf(1.0f, fmaxf(-1.0f, dot(S.n, S.wo))));
       Lk = ltc_lookup(tab, theta, M.alpha);
@@ -451,7 +458,7 @@ __global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params pr
       nshadow = cv_samples<false>(sv, prm, S, M, sv.mats[S.mat].reflectance, Lk, minv, ltc_on,
                                   f3(sv.mats[S.mat].color[0], sv.mats[S.mat].color[1], sv.mats[S.mat].color[2]), key,
                                   meta.y, o_off, cv_neg, nullptr, nullptr, nullptr);
-    else if (surface && SHADER != CKR_SHADER_DIRECT_MISCV)
+    else if (surface && SHADER != CKR_SHADER_DIRECT_MISCV && SHADER != CKR_SHADER_EXPLICIT)
       nshadow = light_samples<SHADER == CKR_SHADER_DIRECT_MIS>(sv, prm, S, M, fcol, beta, key, meta.y, meta.z, o_off,
                                                                nullptr, nullptr, nullptr, false);
     uint32_t sbase = warp_reserve(&P.counts[2], nshadow);
@@ -474,17 +481,18 @@ __global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params pr
       F3 col = f3(mm.color[0], mm.color[1], mm.color[2]);
       add_px(P.accum, meta.x, mulc(col, ltc_term(sv, S, M, Lk, minv, ltc_on) + cv_neg));
     }
-    if (surface && SHADER == CKR_SHADER_DIRECT_MISCV) {
-      // getLightFromMeshSource_Analytic_MISCV (src/lightSources_CV.cpp:399-450).
+    if (surface && (SHADER == CKR_SHADER_DIRECT_MISCV || SHADER == CKR_SHADER_EXPLICIT)) {
+      // getLightFromMeshSource_Analytic_MISCV (src/lightSources_CV.cpp:399-450); at
+      // every vertex of the explicit path loop (shadeDI, src/shader.cpp:100-109).
       F3 G = ltc_term(sv, S, M, Lk, minv, ltc_on);
       // MIS residual over the getSamples set; visibility is 1 in the reference.
       F3 res = f3(0, 0, 0);
       const uint32_t nb = prm.n_brdf, nlobe = (uint32_t)((float)nb * M.spec);
       const uint32_t nls = sv.first_point * prm.n_light;
       for (uint32_t si = 0; si < nls + nb; ++si) {
-        float e0 = ckr_draw_f(key, ctr(meta.y, 0, 3 * si));
-        float e1 = ckr_draw_f(key, ctr(meta.y, 0, 3 * si + 1));
-        float e2 = ckr_draw_f(key, ctr(meta.y, 0, 3 * si + 2));
+        float e0 = ckr_draw_f(key, ctr(meta.y, meta.z, 3 * si));
+        float e1 = ckr_draw_f(key, ctr(meta.y, meta.z, 3 * si + 1));
+        float e2 = ckr_draw_f(key, ctr(meta.y, meta.z, 3 * si + 2));
         F3 w = si < nls ? sample_light(sv, sv.lights[si / prm.n_light], S.x, e0, e1, e2)
                         : (si - nls < nlobe ? sample_lobe(M, S.n, S.wo_ref, S.wo, e1, e2) : sample_cosine(S.n, e1, e2));
         float c = dot(w, S.n);
@@ -508,7 +516,50 @@ __global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params pr
       }
       const ckr_material &mm = sv.mats[S.mat];
       F3 col = f3(mm.color[0], mm.color[1], mm.color[2]);
-      add_px(P.accum, meta.x, mulc(col, res + G));
+      add_px(P.accum, meta.x, mulc(beta, mulc(col, res + G)));
+    }
+    // ---- continuation of the explicit path loop (shadeExplicit, src/shader.cpp:111-207):
+    // Russian roulette 0.3 after the vertex's direct light, then a uniform hemisphere
+    // direction, redrawn while it meets an emitter (emitters only count through the
+    // direct term), traced here; beta *= c 2 pi cos f / 0.7.
+    if (SHADER == CKR_SHADER_EXPLICIT) {
+      extern __shared__ int32_t smem_stack[];
+      uint32_t hit = kMiss;
+      float th = 0.f;
+      F3 wn = f3(0, 0, 0);
+      const bool go = surface && meta.z + 1 < pc.max_depth &&
+                      ckr_draw_f(key, ctr(meta.y, meta.z, kDimRR)) >= prm.rr_prob;
+      // Every lane runs the same number of traversals (the stack is per thread, the
+      // loop has no barrier, but keeping lanes together keeps the warp converged).
+      bool done = !go;
+      for (uint32_t r = 0; r < kExplicitTries; ++r) {
+        if (!done) {
+          wn = sample_hemisphere(S.n, ckr_draw_f(key, ctr(meta.y, meta.z, kDimHemi + 2 * r)),
+                                 ckr_draw_f(key, ctr(meta.y, meta.z, kDimHemi + 2 * r + 1)));
+          RayPre rp = ray_pre(o_off, wn, 0.f);
+          th = 3.0e38f;
+          hit = trace_ray<false>(scene, rp, th, smem_stack + threadIdx.x, TPB, stack_depth);
+          if (hit == kMiss) {
+            done = true;  // escapes the scene
+          } else {
+            const uint32_t hm = (hit & kSphereBit) ? __ldg(&sv.sph_mat[hit & ~kSphereBit]) : __ldg(&sv.tri_mat[hit]);
+            if (sv.mats[hm].light_type == 0) done = true;  // accepted
+            else hit = kMiss;                              // an emitter: draw again
+          }
+        }
+      }
+      if (go && hit != kMiss) {
+        const ckr_material &mm = sv.mats[S.mat];
+        float f = brdf_eval(M, S.n, S.wo_ref, S.wo, wn) * mm.reflectance;
+        float k = 2.0f * kPi * dot(wn, S.n) * f / (1.0f - prm.rr_prob);
+        F3 nb = mulc(beta, f3(mm.color[0], mm.color[1], mm.color[2])) * k;
+        cont = true;
+        next_o = o_off;
+        next_d = make_float4(wn.x, wn.y, wn.z, 3.0e38f);
+        next_b = make_float4(nb.x, nb.y, nb.z, 1.f);
+        P.hit_id[slot] = hit;
+        P.hit_t[slot] = th;
+      }
     }
     // ---- continuation (path tracer) ----
     if (surface && SHADER == CKR_SHADER_PATH) {
@@ -534,8 +585,9 @@ __global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params pr
     }
     uint32_t cbase = warp_reserve(&P.counts[cur ^ 1], cont ? 1u : 0u);
     if (cont) {
-      // Continue in place: the path keeps its slot.
-      P.ray_o[slot] = make_float4(next_o.x, next_o.y, next_o.z, 0.f);
+      // Continue in place: the path keeps its slot.  tmin = -1 marks a ray the
+      // explicit loop has traced already.
+      P.ray_o[slot] = make_float4(next_o.x, next_o.y, next_o.z, SHADER == CKR_SHADER_EXPLICIT ? -1.f : 0.f);
       P.ray_d[slot] = next_d;
       P.beta[slot] = next_b;
       uint32_t nd = meta.z + 1;
@@ -641,7 +693,7 @@ __global__ void __launch_bounds__(TPB) k_shade_nee(ShadeView sv0, Paths P, Param
               F3 contrib = mulc(beta, mulc(fcol, Le)) * (g * (pl / (pl + pb)));
               nshadow = 1;
               so = make_float4(o_off.x, o_off.y, o_off.z, 0.f);
-              sd = make_float4(w.x, w.y, w.z, shadow_tmax(length(Pl - o_off)));
+              sd = shadow_dir(o_off, Pl);
               sc = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
               if (train_frac > 0.f && ckr_draw_f(key, ctr(meta.y, meta.z, kDimTrain)) < train_frac) {
                 // Training sample: the unweighted estimate of cluster j's direct light

@@ -17,6 +17,7 @@ SHADER_DIRECT_MIS = 1
 SHADER_PATH = 2
 SHADER_PATH_NEE = 3
 SHADER_DIRECT_CV = 4
+SHADER_EXPLICIT = 5
 LIGHT_MESH, LIGHT_TRI, LIGHT_SPHERE, LIGHT_POINT = 0, 1, 2, 3
 SCENES = Path(__file__).resolve().parent / "scenes"
 

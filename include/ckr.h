@@ -203,6 +203,11 @@ typedef struct ckr_camera {
  * samples per mesh light, sum Le (V f - f_ltc) cos cos_l / d^2 * area / n, with
  * shadow rays for V. */
 #define CKR_SHADER_DIRECT_CV 4
+/* shadeExplicit (src/shader.cpp:111-207): at every vertex the MISCV direct term
+ * (n_light_samples / n_brdf_samples as in DIRECT_MISCV), then Russian roulette with
+ * rr_prob and a uniform hemisphere continuation redrawn (up to 8 times) while it
+ * meets an emitter; up to max_depth vertices (the reference allows 100). */
+#define CKR_SHADER_EXPLICIT 5
 
 typedef struct ckr_render_cfg {
   uint32_t shader;           /* CKR_SHADER_* */

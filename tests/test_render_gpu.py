@@ -23,6 +23,7 @@ CASES = [
     (S.SHADER_DIRECT_MIS, 4, 10, 60, 1, 1e-4),
     (S.SHADER_PATH, 16, 1, 1, 4, 1e-3),
     (S.SHADER_DIRECT_CV, 4, 25, 0, 1, 1e-4),
+    (S.SHADER_EXPLICIT, 4, 10, 60, 4, 1e-3),
 ]
 
 

@@ -143,3 +143,19 @@ def test_oracle_cv_shader_is_ltc_term_where_unoccluded():
     same = np.all(np.abs(a - b) < 1e-12, axis=2)
     assert 0.5 < same.mean() < 1.0  # most pixels unshadowed, some in the spheres' shadows
     assert np.all(np.isfinite(a))
+
+
+def test_oracle_explicit_path_adds_indirect_light():
+    """shadeExplicit: the MISCV direct term at the first vertex plus indirect light
+    from the hemisphere continuation, so the image is brighter than the direct-only
+    shader's with the same streams at the first vertex."""
+    import oracle as O
+
+    sd = S.load_xml(S.SCENES / "box.xml")
+    cam = sd.camera
+    cam.width = cam.height = 24
+    direct = O.render(sd, cam, S.render_cfg(shader=S.SHADER_DIRECT_MISCV, spp=8, n_light=10, n_brdf=60, seed=1))
+    one = O.render(sd, cam, S.render_cfg(shader=S.SHADER_EXPLICIT, spp=8, max_depth=1, n_light=10, n_brdf=60, seed=1))
+    deep = O.render(sd, cam, S.render_cfg(shader=S.SHADER_EXPLICIT, spp=8, max_depth=6, n_light=10, n_brdf=60, seed=1))
+    assert np.allclose(one, direct)  # one vertex: exactly the direct-only shader
+    assert np.all(np.isfinite(deep)) and deep.mean() > 1.1 * direct.mean()

@@ -35,22 +35,70 @@ namespace {
 
 constexpr int kTPB = 128;
 
+// Closest / any hit with dynamic ray fetching (after Aila and Laine, "Understanding
+// the Efficiency of Ray Traversal on GPUs", HPG 2009): a lane whose ray is finished
+// takes the next ray from a global counter (one atomic per warp refill) instead of
+// idling until its whole warp is done; each loop iteration advances every active lane
+// by one node or one leaf.
+constexpr int kRefill = 8;  // refill once this many lanes of a warp are idle
+
 template <bool ANY>
-__global__ void __launch_bounds__(kTPB) k_trace(SceneView s, const float4 *__restrict__ rays, uint32_t n,
-                                                uint32_t *__restrict__ hit_id, float *__restrict__ hit_t,
-                                                uint8_t *__restrict__ occluded, int depth) {
+__global__ void __launch_bounds__(kTPB) k_trace_dyn(SceneView s, const float4 *__restrict__ rays, uint32_t n,
+                                                    uint32_t *__restrict__ hit_id, float *__restrict__ hit_t,
+                                                    uint8_t *__restrict__ occluded, int depth, uint32_t *next) {
   extern __shared__ int32_t smem_stack[];
   int32_t *stack = smem_stack + threadIdx.x;
-  for (uint32_t i = blockIdx.x * kTPB + threadIdx.x; i < n; i += gridDim.x * kTPB) {
-    float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
-    RayPre r = make_ray(a, b);
-    float tbest = b.w;
-    uint32_t id = trace_ray<ANY>(s, r, tbest, stack, kTPB, depth);
-    if (ANY) {
-      occluded[i] = id != kMiss ? 1 : 0;
-    } else {
-      hit_id[i] = id;
-      hit_t[i] = tbest;
+  const uint32_t lane = threadIdx.x & 31u;
+  RayPre r{};
+  float tbest = 0.f;
+  uint32_t best = kMiss, idx = 0;
+  int32_t node = kDone;
+  int sp = 0;
+  bool active = false, more = true;
+  for (;;) {
+    const unsigned idle = __ballot_sync(0xffffffffu, !active);
+    if (more && (idle == 0xffffffffu || __popc(idle) >= kRefill)) {
+      const uint32_t want = (uint32_t)__popc(idle);
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(next, want);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if ((uint64_t)base + want >= n) more = false;
+      if (!active) {
+        idx = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+        if (idx < n) {
+          float4 a = __ldg(rays + 2 * (size_t)idx), b = __ldg(rays + 2 * (size_t)idx + 1);
+          r = make_ray(a, b);
+          tbest = b.w;
+          best = kMiss;
+          sp = 0;
+          node = s.root;
+          for (uint32_t k = 0; k < s.nsph; ++k) {
+            double t = hit_sphere(r, __ldg(&s.spheres[k]));
+            if (t < (double)tbest) {
+              tbest = (float)t;
+              best = kSphereBit | k;
+              if (ANY) node = kDone;
+            }
+          }
+          active = true;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, active)) {
+      if (!more) break;
+      continue;  // every lane idle: the next iteration refills the whole warp
+    }
+    if (active) {
+      if (node != kDone) trace_step<ANY>(s, r, tbest, best, node, sp, stack, kTPB, depth);
+      if (node == kDone) {
+        if (ANY) {
+          occluded[idx] = best != kMiss ? 1 : 0;
+        } else {
+          hit_id[idx] = best;
+          hit_t[idx] = tbest;
+        }
+        active = false;
+      }
     }
   }
 }
@@ -69,10 +117,10 @@ cudaError_t launch_shape(const ckr_scene *s, uint32_t n, LaunchShape &ls) {
   if (e != cudaSuccess) return e;
   ls.smem = (size_t)stack_depth_of(s) * kTPB * sizeof(int32_t);
   if (ls.smem > 48 * 1024) {
-    e = cudaFuncSetAttribute(k_trace<ANY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls.smem);
+    e = cudaFuncSetAttribute(k_trace_dyn<ANY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls.smem);
     if (e != cudaSuccess) return e;
   }
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<ANY>, kTPB, ls.smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_dyn<ANY>, kTPB, ls.smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   int want = (int)ceil_div(n, kTPB);
@@ -86,9 +134,26 @@ int launch_trace(const ckr_scene *s, const ckr_ray *rays, uint32_t n, uint32_t *
   if (n == 0) return CKR_OK;
   LaunchShape ls;
   CKR_CUDA_TRY(launch_shape<ANY>(s, n, ls));
-  k_trace<ANY><<<ls.grid, kTPB, ls.smem, stream>>>(view_of(s), reinterpret_cast<const float4 *>(rays), n, hit_id,
-                                                   hit_t, occluded, (int)stack_depth_of(s));
-  CKR_CUDA_TRY(cudaGetLastError());
+  // The ray counter is stream-ordered scratch, so concurrent calls on other streams
+  // cannot share it.
+  // Launches cover at most 2^31 rays so that the counter, which overshoots n by at
+  // most one refill per warp, cannot wrap.
+  uint32_t *next = nullptr;
+  CKR_CUDA_TRY(cudaMallocAsync((void **)&next, sizeof(uint32_t), stream));
+  cudaError_t e = cudaSuccess;
+  constexpr uint32_t kChunk = 1u << 31;
+  for (uint32_t off = 0; off < n && e == cudaSuccess; off += std::min(n - off, kChunk)) {
+    const uint32_t m = std::min(n - off, kChunk);
+    e = cudaMemsetAsync(next, 0, sizeof(uint32_t), stream);
+    if (e != cudaSuccess) break;
+    k_trace_dyn<ANY><<<ls.grid, kTPB, ls.smem, stream>>>(
+        view_of(s), reinterpret_cast<const float4 *>(rays + off), m, ANY ? nullptr : hit_id + off,
+        ANY ? nullptr : hit_t + off, ANY ? occluded + off : nullptr, (int)stack_depth_of(s), next);
+    e = cudaGetLastError();
+    if (n - off <= kChunk) break;
+  }
+  cudaFreeAsync(next, stream);
+  CKR_CUDA_TRY(e);
   return CKR_OK;
 }
 

@@ -143,6 +143,57 @@ __device__ __forceinline__ void hit_children(const RayPre &r, float4 n0, float4 
   t1 = en <= ex ? en : __int_as_float(0x7f800000);
 }
 
+// One traversal step of a ray: an interior node (both child boxes; the nearer hit
+// child next, the farther pushed) or a leaf (its triangles, then a pop).  `node` is
+// kDone when the ray is finished.  Stack as in trace_ray.
+template <bool ANY>
+__device__ __forceinline__ void trace_step(const SceneView &s, const RayPre &r, float &tbest, uint32_t &best,
+                                           int32_t &node, int &sp, int32_t *stack, int stride, int depth) {
+  if (node >= 0) {
+    const float4 *np = s.nodes + 4 * (size_t)node;
+    float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
+    float t0, t1;
+    hit_children(r, n0, n1, n2, tbest, t0, t1);
+    int32_t l0 = __float_as_int(n3.x), l1 = __float_as_int(n3.y);
+    bool h0 = t0 != __int_as_float(0x7f800000), h1 = t1 != __int_as_float(0x7f800000);
+    if (h0 && h1) {
+      int32_t near = l0, far = l1;
+      if (t1 < t0) { near = l1; far = l0; }
+      if (sp >= depth) {
+        atomicCAS(s.status, 0, -4 /* CKR_ERR_STACK_OVERFLOW */);
+        best = kMiss;
+        node = kDone;
+        return;
+      }
+      stack[sp * stride] = far;
+      ++sp;
+      node = near;
+    } else if (h0 | h1) {
+      node = h0 ? l0 : l1;
+    } else {
+      node = sp > 0 ? stack[--sp * stride] : kDone;
+    }
+    return;
+  }
+  // Leaf: ~node = (first << 3) | (count - 1).
+  uint32_t code = ~(uint32_t)node;
+  uint32_t first = code >> 3, count = (code & 7u) + 1u;
+  const float4 *tp = s.tris + 3 * (size_t)first;
+  for (uint32_t k = 0; k < count; ++k) {
+    float4 v0 = __ldg(tp + 3 * k), v1 = __ldg(tp + 3 * k + 1), v2 = __ldg(tp + 3 * k + 2);
+    float t;
+    if (hit_triangle(r, v0, v1, v2, tbest, t)) {
+      tbest = t;
+      best = __float_as_uint(v0.w);
+      if (ANY) {
+        node = kDone;
+        return;
+      }
+    }
+  }
+  node = sp > 0 ? stack[--sp * stride] : kDone;
+}
+
 // Traces one ray.  ANY: stop at the first hit.  The stack lives in shared
 // memory, one column per thread (stack[level * stride]), `depth` entries.
 // Returns the hit id (kMiss, triangle index, or kSphereBit | sphere index)

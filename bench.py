@@ -591,10 +591,11 @@ def main():
         dist.destroy_process_group()
         return
 
-    # Roofline: algorithmic bytes per ray from the replayed box/triangle counts.
+    # Roofline: algorithmic bytes per ray from the replayed node/triangle counts
+    # (80-byte wide nodes, 36 bytes of vertices per triangle).
     sample = np.ascontiguousarray(closest[::16])
-    mean_boxes, mean_tris = scene.stats(sample)
-    bytes_per_ray = 32 + 8 + 32 * mean_boxes + 36 * mean_tris
+    mean_nodes, mean_tris = scene.stats(sample)
+    bytes_per_ray = 32 + 8 + 80 * mean_nodes + 36 * mean_tris
     achieved = n * bytes_per_ray / (step_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
     traffic = traffic_from_profile()
@@ -603,12 +604,13 @@ def main():
         "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "rays_per_step": n, "triangles": int(info.ntri),
-                   "bvh": f"binned SAH, leaf<={args.leaf}, {info.nnodes} interior nodes, depth {info.max_depth}",
+                   "bvh": (f"binned SAH, leaf<={args.leaf} ({info.nnodes_binary} binary nodes), collapsed to "
+                           f"8-wide, 8-bit quantised boxes: {info.nnodes} wide nodes, depth {info.max_depth}"),
                    "bvh_build_ms": round(info.build_ms, 1), "l2": "inputs larger than L2 (rays 256 MiB), no flush",
                    "parallelism": f"replica x{world}"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
-                     "bytes_per_ray": round(bytes_per_ray, 1), "mean_boxes": round(mean_boxes, 2),
+                     "bytes_per_ray": round(bytes_per_ray, 1), "mean_wide_nodes": round(mean_nodes, 2),
                      "mean_tris": round(mean_tris, 3)},
         "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 8},
         "gpu_launches": args.steps,

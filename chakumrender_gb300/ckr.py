@@ -32,7 +32,7 @@ class BuildParams(C.Structure):
 
 class SceneInfo(C.Structure):
     _fields_ = [("ntri", C.c_uint32), ("nsph", C.c_uint32), ("nnodes", C.c_uint32), ("nleaves", C.c_uint32),
-                ("max_depth", C.c_uint32), ("reserved", C.c_uint32), ("device_bytes", C.c_uint64),
+                ("max_depth", C.c_uint32), ("nnodes_binary", C.c_uint32), ("device_bytes", C.c_uint64),
                 ("build_ms", C.c_double)]
 
 

@@ -135,7 +135,7 @@ template <int TPB>
 int enqueue(ckr_batch *b, JobSet &set, bool pack, size_t wave, cudaStream_t stream, uint32_t *launches) {
   ckr_scene *s = b->scene;
   const int depth = (int)stack_depth_of(s);
-  const size_t smem = (size_t)depth * TPB * sizeof(int32_t);
+  const size_t smem = (size_t)depth * TPB * sizeof(uint2);
   if (smem > 48 * 1024) {
     CKR_CUDA_TRY(cudaFuncSetAttribute(k_extend<TPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CKR_CUDA_TRY(cudaFuncSetAttribute(k_shadow<TPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -8,8 +8,9 @@
 // Algorithm: top-down binned SAH (Wald 2007, "On fast construction of
 // SAH-based bounding volume hierarchies"), bins on all three centroid axes,
 // costs C_trav = 1 and C_isect = 1 per triangle; large subtrees are built on
-// separate threads.  The tree is then flattened depth-first into nodes that
-// hold both child boxes (Aila and Laine 2009), leaves inlined as links.
+// separate threads.  The binary tree is then collapsed into eight-wide nodes
+// with 8-bit quantised child boxes (Ylitie, Karras, Laine, HPG 2017; layout in
+// bvh_build.h).
 #include "bvh_build.h"
 
 #include <algorithm>
@@ -175,6 +176,178 @@ struct Builder {
   }
 };
 
+// Exact position of a quantised plane, p + q 2^e.  Exact in double: p and the
+// bound it is compared with are floats within the node's extent of each other
+// and q 2^e has at most 8 significant bits.
+inline double plane(float p, uint32_t q, int e) { return (double)p + std::ldexp((double)q, e); }
+
+// One child of a wide node under construction: an interior node of the binary
+// tree, or a run of at most kWideLeafMax triangles of one of its leaves.
+struct Entry {
+  Box box;
+  uint32_t tnode;         // interior: binary-tree node
+  uint32_t begin, count;  // leaf: prims[begin, begin + count); count 0 for interior
+};
+
+void entries_of(const Builder &b, uint32_t ti, std::vector<Entry> &out) {
+  const TNode &n = b.pool[ti];
+  if (n.count == 0) {
+    out.push_back({n.box, ti, 0, 0});
+    return;
+  }
+  for (uint32_t i = n.begin; i < n.begin + n.count; i += kWideLeafMax) {
+    Entry e{};
+    e.count = std::min(kWideLeafMax, n.begin + n.count - i);
+    e.begin = i;
+    e.box.reset();
+    for (uint32_t k = i; k < i + e.count; ++k) e.box.grow(b.prims[k].box);
+    out.push_back(e);
+  }
+}
+
+uint32_t slots_of(const TNode &n) { return n.count ? (n.count + kWideLeafMax - 1) / kWideLeafMax : 1; }
+
+// Collapses the binary tree into wide nodes.  Each wide node starts from the two
+// children of a binary node and repeatedly opens the child with the largest
+// surface area while the children still fit in eight slots.  Children go to
+// slots by a greedy assignment on cost(child, slot) = (centroid - node centre) .
+// dir(slot), dir = the octant's signs, so that slot o holds the child nearest the
+// start of rays travelling in octant o.  Boxes are quantised outward.
+void collapse(const Builder &b, const float *tri9, FlatBvh &out) {
+  const uint32_t n = (uint32_t)b.prims.size();
+  out.tris.reserve((size_t)n * 12);
+  out.nnodes_binary = 0;
+  for (uint32_t i = 0; i < (uint32_t)b.next.load(); ++i)
+    if (b.pool[i].count == 0) out.nnodes_binary++;
+  struct Work {
+    uint32_t tnode, index, depth;
+  };
+  std::vector<Work> work{{0, 0, 1}};
+  out.nnodes = 1;
+  out.root = 0;
+  std::vector<Entry> kids;
+  while (!work.empty()) {
+    Work wk = work.back();
+    work.pop_back();
+    out.max_depth = std::max(out.max_depth, wk.depth);
+    const TNode &tn = b.pool[wk.tnode];
+    kids.clear();
+    if (tn.count > 0) {
+      entries_of(b, wk.tnode, kids);  // the whole tree is one leaf
+    } else {
+      entries_of(b, tn.left, kids);
+      entries_of(b, tn.left + 1, kids);
+    }
+    for (;;) {
+      int best = -1;
+      float best_area = -1.f;
+      for (size_t k = 0; k < kids.size(); ++k) {
+        if (kids[k].count) continue;
+        const TNode &c = b.pool[kids[k].tnode];
+        uint32_t need = (uint32_t)kids.size() - 1 + slots_of(b.pool[c.left]) + slots_of(b.pool[c.left + 1]);
+        float area = c.box.area();
+        if (need <= 8 && area > best_area) {
+          best_area = area;
+          best = (int)k;
+        }
+      }
+      if (best < 0) break;
+      uint32_t ti = kids[best].tnode;
+      kids.erase(kids.begin() + best);
+      entries_of(b, b.pool[ti].left, kids);
+      entries_of(b, b.pool[ti].left + 1, kids);
+    }
+    // Node box and quantisation grid.
+    Box nb;
+    nb.reset();
+    for (const Entry &e : kids) nb.grow(e.box);
+    float centre[3];
+    for (int a = 0; a < 3; ++a) centre[a] = 0.5f * nb.lo[a] + 0.5f * nb.hi[a];
+    // Greedy slot assignment over all (child, slot) pairs, cheapest first.
+    struct Pair {
+      float cost;
+      int kid, slot;
+    };
+    Pair pairs[64];
+    int np = 0;
+    for (int k = 0; k < (int)kids.size(); ++k) {
+      float c[3];
+      for (int a = 0; a < 3; ++a) c[a] = 0.5f * kids[k].box.lo[a] + 0.5f * kids[k].box.hi[a] - centre[a];
+      for (int slot = 0; slot < 8; ++slot) {
+        float cost = ((slot & 4) ? -c[0] : c[0]) + ((slot & 2) ? -c[1] : c[1]) + ((slot & 1) ? -c[2] : c[2]);
+        pairs[np++] = {cost, k, slot};
+      }
+    }
+    std::stable_sort(pairs, pairs + np, [](const Pair &x, const Pair &y) { return x.cost < y.cost; });
+    int slot_kid[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+    bool placed[8] = {false, false, false, false, false, false, false, false};
+    for (int i = 0; i < np; ++i)
+      if (slot_kid[pairs[i].slot] < 0 && !placed[pairs[i].kid]) {
+        slot_kid[pairs[i].slot] = pairs[i].kid;
+        placed[pairs[i].kid] = true;
+      }
+    uint32_t w[kWideWords] = {};
+    std::memcpy(&w[0], &nb.lo[0], 12);
+    int e[3];
+    for (int a = 0; a < 3; ++a) {
+      const double p = nb.lo[a], hi = nb.hi[a], ext = hi - p;
+      int ex = -126;
+      if (ext > 0.0) {
+        std::frexp(ext / 255.0, &ex);  // 2^ex > ext / 255
+        while (ex > -126 && p + 255.0 * std::ldexp(1.0, ex - 1) >= hi) --ex;
+        while (p + 255.0 * std::ldexp(1.0, ex) < hi) ++ex;
+      }
+      e[a] = std::max(-126, std::min(127, ex));
+      w[3] |= (uint32_t)(e[a] + 127) << (8 * a);
+    }
+    uint8_t meta[8] = {}, q[6][8] = {};
+    uint32_t imask = 0, nint = 0;
+    const uint32_t child_base = out.nnodes, tri_base = (uint32_t)(out.tris.size() / 12);
+    for (int slot = 0; slot < 8; ++slot) {
+      if (slot_kid[slot] < 0) continue;
+      const Entry &c = kids[slot_kid[slot]];
+      for (int a = 0; a < 3; ++a) {
+        const double p = nb.lo[a], step = std::ldexp(1.0, e[a]);
+        double lo = std::floor(((double)c.box.lo[a] - p) / step), hi = std::ceil(((double)c.box.hi[a] - p) / step);
+        uint32_t ql = (uint32_t)std::max(0.0, std::min(255.0, lo)), qh = (uint32_t)std::max(0.0, std::min(255.0, hi));
+        while (ql > 0 && plane(nb.lo[a], ql, e[a]) > (double)c.box.lo[a]) --ql;
+        while (qh < 255 && plane(nb.lo[a], qh, e[a]) < (double)c.box.hi[a]) ++qh;
+        q[2 * a][slot] = (uint8_t)ql;
+        q[2 * a + 1][slot] = (uint8_t)qh;
+      }
+      if (c.count == 0) {
+        imask |= 1u << slot;
+        meta[slot] = (uint8_t)(0x38 + slot);
+        ++nint;
+      } else {
+        const uint32_t off = (uint32_t)(out.tris.size() / 12) - tri_base;
+        meta[slot] = (uint8_t)((((1u << c.count) - 1u) << 5) | off);
+        for (uint32_t i = c.begin; i < c.begin + c.count; ++i) {
+          const float *t = tri9 + 9 * (size_t)b.prims[i].id;
+          float rec[12] = {t[0], t[1], t[2], 0.f, t[3], t[4], t[5], 0.f, t[6], t[7], t[8], 0.f};
+          std::memcpy(&rec[3], &b.prims[i].id, 4);
+          out.tris.insert(out.tris.end(), rec, rec + 12);
+        }
+        out.nleaves++;
+      }
+    }
+    w[3] |= imask << 24;
+    w[4] = child_base;
+    w[5] = tri_base;
+    std::memcpy(&w[6], meta, 8);
+    std::memcpy(&w[8], q, 48);
+    if (out.nodes.size() < (size_t)(wk.index + 1) * kWideWords) out.nodes.resize((size_t)(wk.index + 1) * kWideWords);
+    std::memcpy(&out.nodes[(size_t)wk.index * kWideWords], w, sizeof(w));
+    // Interior children get consecutive indices in slot order; the first slot's
+    // subtree is processed next (depth first).
+    out.nnodes += nint;
+    uint32_t k = nint;
+    for (int slot = 7; slot >= 0; --slot)
+      if ((imask >> slot) & 1u) work.push_back({kids[slot_kid[slot]].tnode, child_base + --k, wk.depth + 1});
+  }
+  out.nodes.resize((size_t)out.nnodes * kWideWords);
+}
+
 }  // namespace
 
 int build_bvh(const float *tri9, uint32_t ntri, const ckr_build_params &params, FlatBvh &out) {
@@ -214,96 +387,97 @@ int build_bvh(const float *tri9, uint32_t ntri, const ckr_build_params &params, 
   for (const Prim &p : b.prims) b.pool[0].box.grow(p.box);
   b.build(0, 0, n);
 
-  // Flatten: triangles in leaf order, nodes depth-first.
-  out.tris.reserve((size_t)n * 12);
-  struct Emit {
-    static void tris(const Builder &b, const TNode &leaf, const float *tri9, std::vector<float> &dst) {
-      for (uint32_t i = leaf.begin; i < leaf.begin + leaf.count; ++i) {
-        const float *t = tri9 + 9 * (size_t)b.prims[i].id;
-        float rec[12] = {t[0], t[1], t[2], 0.f, t[3], t[4], t[5], 0.f, t[6], t[7], t[8], 0.f};
-        std::memcpy(&rec[3], &b.prims[i].id, 4);
-        dst.insert(dst.end(), rec, rec + 12);
-      }
-    }
-  };
-  // Iterative DFS that assigns node indices in pre-order and emits leaves in
-  // the same order the recursive layout would.
-  struct Frame {
-    uint32_t tnode, depth;
-    int32_t parent;
-    int slot;
-  };
-  std::vector<Frame> stack;
-  stack.push_back({0, 0, -1, 0});
-  std::vector<int32_t> links;  // per flat node: link0, link1
-  while (!stack.empty()) {
-    Frame f = stack.back();
-    stack.pop_back();
-    const TNode &tn = b.pool[f.tnode];
-    int32_t link;
-    if (tn.count > 0) {
-      uint32_t first = (uint32_t)(out.tris.size() / 12);
-      Emit::tris(b, tn, tri9, out.tris);
-      out.nleaves++;
-      link = leaf_link(first, tn.count);
-    } else {
-      uint32_t my = out.nnodes++;
-      if (f.depth + 1 > out.max_depth) out.max_depth = f.depth + 1;
-      out.nodes.resize((size_t)out.nnodes * 16, 0.f);
-      const Box &c0 = b.pool[tn.left].box, &c1 = b.pool[tn.left + 1].box;
-      float *r = &out.nodes[(size_t)my * 16];
-      r[0] = c0.lo[0]; r[1] = c0.hi[0]; r[2] = c0.lo[1]; r[3] = c0.hi[1];
-      r[4] = c1.lo[0]; r[5] = c1.hi[0]; r[6] = c1.lo[1]; r[7] = c1.hi[1];
-      r[8] = c0.lo[2]; r[9] = c0.hi[2]; r[10] = c1.lo[2]; r[11] = c1.hi[2];
-      // Right child pushed first so the left subtree is laid out first.
-      stack.push_back({tn.left + 1, f.depth + 1, (int32_t)my, 1});
-      stack.push_back({tn.left, f.depth + 1, (int32_t)my, 0});
-      link = (int32_t)my;
-    }
-    if (f.parent < 0) {
-      out.root = link;
-    } else {
-      std::memcpy(&out.nodes[(size_t)f.parent * 16 + 12 + f.slot], &link, 4);
-    }
-  }
+  collapse(b, tri9, out);
   return validate_bvh(out) ? CKR_OK : CKR_ERR_INVALID_ARGUMENT;
 }
 
 bool validate_bvh(const FlatBvh &b) {
-  // Every interior node is referenced exactly once (the root by `root`), every
-  // leaf range lies inside the triangle array, and the ranges tile it exactly.
-  uint32_t ntri = (uint32_t)(b.tris.size() / 12);
-  if (b.root == FlatBvh::kEmptyRoot) return ntri == 0 && b.nnodes == 0;
-  std::vector<uint8_t> seen(b.nnodes, 0);
+  const uint32_t ntri = (uint32_t)(b.tris.size() / 12);
+  if (b.root == FlatBvh::kEmptyRoot) return ntri == 0 && b.nnodes == 0 && b.nodes.empty();
+  if (b.root != 0 || b.nnodes == 0 || b.nodes.size() != (size_t)b.nnodes * kWideWords) return false;
+  std::vector<uint32_t> level(b.nnodes, 0);
   std::vector<uint8_t> covered(ntri, 0);
-  std::vector<std::pair<int32_t, uint32_t>> stack{{b.root, 1}};
-  uint32_t depth_max = 0;
-  while (!stack.empty()) {
-    auto [link, depth] = stack.back();
-    stack.pop_back();
-    if (link >= 0) {
-      if ((uint32_t)link >= b.nnodes || seen[link]) return false;
-      seen[link] = 1;
-      depth_max = std::max(depth_max, depth);
-      int32_t l[2];
-      std::memcpy(l, &b.nodes[(size_t)link * 16 + 12], 8);
-      stack.push_back({l[0], depth + 1});
-      stack.push_back({l[1], depth + 1});
-    } else {
-      uint32_t code = ~(uint32_t)link;
-      uint32_t first = code >> 3, count = (code & 7u) + 1u;
-      if ((uint64_t)first + count > ntri) return false;
-      for (uint32_t i = first; i < first + count; ++i) {
-        if (covered[i]) return false;
-        covered[i] = 1;
+  level[0] = 1;
+  uint32_t depth_max = 0, leaves = 0;
+  // Top-down: children lie after their parent, so one pass in index order sees
+  // every parent before its children.
+  for (uint32_t i = 0; i < b.nnodes; ++i) {
+    if (level[i] == 0) return false;  // unreachable node
+    depth_max = std::max(depth_max, level[i]);
+    const uint32_t *w = &b.nodes[(size_t)i * kWideWords];
+    const uint32_t imask = w[3] >> 24, child_base = w[4], tri_base = w[5];
+    uint8_t meta[8];
+    std::memcpy(meta, &w[6], 8);
+    uint32_t nint = 0;
+    for (uint32_t slot = 0; slot < 8; ++slot) {
+      const uint32_t m = meta[slot];
+      const bool inner = (imask >> slot) & 1u;
+      if (inner) {
+        if (m != 0x38u + slot) return false;
+        uint64_t c = (uint64_t)child_base + nint++;
+        if (c >= b.nnodes || c <= i || level[c] != 0) return false;
+        level[c] = level[i] + 1;
+      } else if (m != 0) {
+        const uint32_t bits = m >> 5, off = m & 31u;
+        const uint32_t cnt = bits == 1 ? 1 : bits == 3 ? 2 : bits == 7 ? 3 : 0;
+        if (cnt == 0 || off + cnt > 24 || (uint64_t)tri_base + off + cnt > ntri) return false;
+        for (uint32_t k = tri_base + off; k < tri_base + off + cnt; ++k) {
+          if (covered[k]) return false;
+          covered[k] = 1;
+        }
+        leaves++;
       }
     }
   }
   for (uint8_t c : covered)
     if (!c) return false;
-  for (uint8_t s : seen)
-    if (!s) return false;
-  return depth_max == b.max_depth;
+  // Bottom-up: exact boxes, and each one inside its quantised slot box.
+  std::vector<float> box((size_t)b.nnodes * 6);
+  for (uint32_t i = b.nnodes; i-- > 0;) {
+    const uint32_t *w = &b.nodes[(size_t)i * kWideWords];
+    const uint32_t imask = w[3] >> 24, child_base = w[4], tri_base = w[5];
+    uint8_t meta[8], q[6][8];
+    std::memcpy(meta, &w[6], 8);
+    std::memcpy(q, &w[8], 48);
+    float p[3];
+    std::memcpy(p, &w[0], 12);
+    int e[3];
+    for (int a = 0; a < 3; ++a) e[a] = (int)((w[3] >> (8 * a)) & 0xffu) - 127;
+    float *nb = &box[(size_t)i * 6];
+    for (int a = 0; a < 3; ++a) {
+      nb[a] = std::numeric_limits<float>::infinity();
+      nb[3 + a] = -std::numeric_limits<float>::infinity();
+    }
+    uint32_t nint = 0;
+    for (uint32_t slot = 0; slot < 8; ++slot) {
+      const uint32_t m = meta[slot];
+      if (m == 0) continue;
+      float cb[6];
+      if ((imask >> slot) & 1u) {
+        std::memcpy(cb, &box[(size_t)(child_base + nint++) * 6], sizeof(cb));
+      } else {
+        const uint32_t bits = m >> 5, off = m & 31u, cnt = bits == 1 ? 1 : bits == 3 ? 2 : 3;
+        for (int a = 0; a < 3; ++a) {
+          cb[a] = std::numeric_limits<float>::infinity();
+          cb[3 + a] = -std::numeric_limits<float>::infinity();
+        }
+        for (uint32_t k = tri_base + off; k < tri_base + off + cnt; ++k)
+          for (int v = 0; v < 3; ++v)
+            for (int a = 0; a < 3; ++a) {
+              float x = b.tris[(size_t)k * 12 + 4 * v + a];
+              cb[a] = std::min(cb[a], x);
+              cb[3 + a] = std::max(cb[3 + a], x);
+            }
+      }
+      for (int a = 0; a < 3; ++a) {
+        if (plane(p[a], q[2 * a][slot], e[a]) > (double)cb[a]) return false;
+        if (plane(p[a], q[2 * a + 1][slot], e[a]) < (double)cb[3 + a]) return false;
+        nb[a] = std::min(nb[a], cb[a]);
+        nb[3 + a] = std::max(nb[3 + a], cb[3 + a]);
+      }
+    }
+  }
+  return depth_max == b.max_depth && leaves == b.nleaves;
 }
 
 }  // namespace ckr

@@ -156,7 +156,7 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   SceneView sv = view_of(s);
   ShadeView shv = shade_view_of(s);
   int depth = (int)stack_depth_of(s);
-  size_t smem = (size_t)depth * kRTPB * sizeof(int32_t);
+  size_t smem = (size_t)depth * kRTPB * sizeof(uint2);
   if (smem > 48 * 1024) {
     CKR_CUDA_TRY(cudaFuncSetAttribute(k_extend<kRTPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CKR_CUDA_TRY(cudaFuncSetAttribute(k_shadow<kRTPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -410,7 +410,7 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
   ShadeView shv = shade_view_of(s);
   const LtcEntry *ltc = g_noalloc_ltc_dev[dev];
   int depth = (int)stack_depth_of(s);
-  size_t smem = (size_t)depth * kRTPB * sizeof(int32_t);
+  size_t smem = (size_t)depth * kRTPB * sizeof(uint2);
   if (smem > 48 * 1024) {
     CKR_CUDA_TRY(cudaFuncSetAttribute(k_extend<kRTPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CKR_CUDA_TRY(cudaFuncSetAttribute(k_shadow<kRTPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -55,9 +55,10 @@ struct ckr_scene {
   ckr::DevBuf<float4> nodes, tris, spheres;
   ckr::DevBuf<int> status;
   int32_t root = ckr::kDone;
-  uint32_t ntri = 0, nsph = 0, nnodes = 0, nleaves = 0, max_depth = 0;
+  uint32_t ntri = 0, nsph = 0, nnodes = 0, nleaves = 0, max_depth = 0, nnodes_binary = 0;
   double build_ms = 0.0;
-  std::vector<float> host_nodes, host_tris;  // kept for the host statistics replay
+  std::vector<uint32_t> host_nodes;          // wide nodes, kept for the host statistics replay
+  std::vector<float> host_tris;
   std::vector<float> host_spheres;
   // Shading data (ckr_scene_create_ex only).
   bool has_shading = false;

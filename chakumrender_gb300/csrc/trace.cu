@@ -39,22 +39,21 @@ constexpr int kTPB = 128;
 // the Efficiency of Ray Traversal on GPUs", HPG 2009): a lane whose ray is finished
 // takes the next ray from a global counter (one atomic per warp refill) instead of
 // idling until its whole warp is done; each loop iteration advances every active lane
-// by one node or one leaf.
+// by one wide node and/or one triangle (trace_step).
 constexpr int kRefill = 8;  // refill once this many lanes of a warp are idle
 
 template <bool ANY>
 __global__ void __launch_bounds__(kTPB) k_trace_dyn(SceneView s, const float4 *__restrict__ rays, uint32_t n,
                                                     uint32_t *__restrict__ hit_id, float *__restrict__ hit_t,
                                                     uint8_t *__restrict__ occluded, int depth, uint32_t *next) {
-  extern __shared__ int32_t smem_stack[];
-  int32_t *stack = smem_stack + threadIdx.x;
+  extern __shared__ uint2 smem_trav[];
+  uint2 *stack = smem_trav + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31u;
   RayPre r{};
   float tbest = 0.f;
   uint32_t best = kMiss, idx = 0;
-  int32_t node = kDone;
-  int sp = 0;
-  bool active = false, more = true;
+  Trav st{};
+  bool active = false, live = false, more = true;
   for (;;) {
     const unsigned idle = __ballot_sync(0xffffffffu, !active);
     if (more && (idle == 0xffffffffu || __popc(idle) >= kRefill)) {
@@ -70,16 +69,8 @@ __global__ void __launch_bounds__(kTPB) k_trace_dyn(SceneView s, const float4 *_
           r = make_ray(a, b);
           tbest = b.w;
           best = kMiss;
-          sp = 0;
-          node = s.root;
-          for (uint32_t k = 0; k < s.nsph; ++k) {
-            double t = hit_sphere(r, __ldg(&s.spheres[k]));
-            if (t < (double)tbest) {
-              tbest = (float)t;
-              best = kSphereBit | k;
-              if (ANY) node = kDone;
-            }
-          }
+          st = trav_start(s, r);
+          live = trace_spheres<ANY>(s, r, tbest, best);
           active = true;
         }
       }
@@ -89,8 +80,8 @@ __global__ void __launch_bounds__(kTPB) k_trace_dyn(SceneView s, const float4 *_
       continue;  // every lane idle: the next iteration refills the whole warp
     }
     if (active) {
-      if (node != kDone) trace_step<ANY>(s, r, tbest, best, node, sp, stack, kTPB, depth);
-      if (node == kDone) {
+      if (live) live = trace_step<ANY>(s, r, tbest, best, st, stack, kTPB, depth);
+      if (!live) {
         if (ANY) {
           occluded[idx] = best != kMiss ? 1 : 0;
         } else {
@@ -115,7 +106,7 @@ cudaError_t launch_shape(const ckr_scene *s, uint32_t n, LaunchShape &ls) {
   if (e != cudaSuccess) return e;
   e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
-  ls.smem = (size_t)stack_depth_of(s) * kTPB * sizeof(int32_t);
+  ls.smem = (size_t)stack_depth_of(s) * kTPB * sizeof(uint2);
   if (ls.smem > 48 * 1024) {
     e = cudaFuncSetAttribute(k_trace_dyn<ANY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls.smem);
     if (e != cudaSuccess) return e;
@@ -189,13 +180,14 @@ extern "C" int ckr_scene_create(const float *tri9, uint32_t ntri, const float *s
   s->nnodes = bvh.nnodes;
   s->nleaves = bvh.nleaves;
   s->max_depth = bvh.max_depth;
+  s->nnodes_binary = bvh.nnodes_binary;
   s->build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   size_t nn = std::max<size_t>(1, bvh.nodes.size() / 4), nt = std::max<size_t>(1, bvh.tris.size() / 4);
   if (s->nodes.reserve(nn) != cudaSuccess || s->tris.reserve(nt) != cudaSuccess ||
       s->spheres.reserve(std::max<uint32_t>(1, nsph)) != cudaSuccess || s->status.reserve(1) != cudaSuccess)
     return fail(CKR_ERR_OUT_OF_MEMORY);
-  if (!bvh.nodes.empty() &&
-      cudaMemcpy(s->nodes.ptr, bvh.nodes.data(), bvh.nodes.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+  if (!bvh.nodes.empty() && cudaMemcpy(s->nodes.ptr, bvh.nodes.data(), bvh.nodes.size() * sizeof(uint32_t),
+                                        cudaMemcpyHostToDevice) != cudaSuccess)
     return fail(CKR_ERR_CUDA);
   if (!bvh.tris.empty() &&
       cudaMemcpy(s->tris.ptr, bvh.tris.data(), bvh.tris.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
@@ -231,6 +223,7 @@ extern "C" int ckr_scene_get_info(const ckr_scene *s, ckr_scene_info *out) {
   out->nnodes = s->nnodes;
   out->nleaves = s->nleaves;
   out->max_depth = s->max_depth;
+  out->nnodes_binary = s->nnodes_binary;
   out->device_bytes = s->nodes.bytes() + s->tris.bytes() + s->spheres.bytes();
   out->build_ms = s->build_ms;
   return CKR_OK;
@@ -332,7 +325,7 @@ extern "C" int ckr_trace_any_host(ckr_scene *s, const ckr_ray *rays, uint32_t n,
 
 namespace ckr {
 // Accessors for the host statistics replay (trace_stats.cpp).
-void scene_host_arrays(const ckr_scene *s, const float **nodes, const float **tris, const float **spheres,
+void scene_host_arrays(const ckr_scene *s, const uint32_t **nodes, const float **tris, const float **spheres,
                        int32_t *root, uint32_t *nsph, uint32_t *depth) {
   *nodes = s->host_nodes.data();
   *tris = s->host_tris.data();

@@ -21,10 +21,10 @@ constexpr uint32_t kSphereBit = 0x80000000u;
 constexpr float kRobustFar = 1.0000003576278687f;
 
 struct SceneView {
-  const float4 *nodes;    // 4 words per interior node
+  const float4 *nodes;    // 5 words per wide node (layout in bvh_build.h)
   const float4 *tris;     // 3 words per triangle, leaf order
   const float4 *spheres;  // centre.xyz, radius
-  int32_t root;
+  int32_t root;           // 0, or kDone when no triangle is indexed
   uint32_t nsph;
   int *status;            // first device error (CKR_ERR_*), 0 when none
 };
@@ -36,14 +36,28 @@ struct RayPre {
   float mx0, mx1, mx2;     // shear rows: sheared x = mx . (v - o)
   float my0, my1, my2;
   float mz0, mz1, mz2;
+  uint32_t oct;            // 7 ^ octant (bit 2: dx < 0, bit 1: dy < 0, bit 0: dz < 0)
 };
 
+// Largest |1/d| the slab tests use.  A ray with d = +-0 on an axis must keep an
+// exact test on that axis (its origin inside the slab or not); with 1/d = inf
+// the quantised test would compute 0 * inf = NaN, drop the axis, and visit every
+// node the other two axes admit.  With 1/d capped the test is that of a ray
+// tilted by at most 1e-20 per unit length, which moves no hit by a
+// representable amount at scene coordinates.
+constexpr float kMaxInvDir = 1e20f;
+
 #if defined(__CUDACC__)
+__device__ __forceinline__ float inv_dir(float d) {
+  const float i = 1.0f / d;
+  return fabsf(i) > kMaxInvDir ? copysignf(kMaxInvDir, i) : i;
+}
+
 __device__ __forceinline__ RayPre make_ray(float4 a, float4 b) {
   RayPre r;
   r.ox = a.x; r.oy = a.y; r.oz = a.z; r.tmin = a.w;
   r.dx = b.x; r.dy = b.y; r.dz = b.z;
-  r.ix = 1.0f / r.dx; r.iy = 1.0f / r.dy; r.iz = 1.0f / r.dz;
+  r.ix = inv_dir(r.dx); r.iy = inv_dir(r.dy); r.iz = inv_dir(r.dz);
   float ax = fabsf(r.dx), ay = fabsf(r.dy), az = fabsf(r.dz);
   int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
   int kx = kz == 2 ? 0 : kz + 1;
@@ -62,6 +76,7 @@ __device__ __forceinline__ RayPre make_ray(float4 a, float4 b) {
   r.mz0 = kz == 0 ? sz : 0.f;
   r.mz1 = kz == 1 ? sz : 0.f;
   r.mz2 = kz == 2 ? sz : 0.f;
+  r.oct = 7u ^ ((r.dx < 0.f ? 4u : 0u) | (r.dy < 0.f ? 2u : 0u) | (r.dz < 0.f ? 1u : 0u));
   return r;
 }
 
@@ -124,133 +139,157 @@ __device__ __forceinline__ double hit_sphere(const RayPre &r, float4 s) {
   return t > eps ? t : 1e300;
 }
 
-// Both child boxes of an interior node; returns entry distances (or +inf on a miss).
-__device__ __forceinline__ void hit_children(const RayPre &r, float4 n0, float4 n1, float4 n2,
-                                             float tbest, float &t0, float &t1) {
-  float lx = (n0.x - r.ox) * r.ix, hx = (n0.y - r.ox) * r.ix;
-  float ly = (n0.z - r.oy) * r.iy, hy = (n0.w - r.oy) * r.iy;
-  float lz = (n2.x - r.oz) * r.iz, hz = (n2.y - r.oz) * r.iz;
-  float en = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fmaxf(fminf(lz, hz), r.tmin));
-  float ex = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fmaxf(lz, hz)) * kRobustFar;
-  ex = fminf(ex, tbest);
-  t0 = en <= ex ? en : __int_as_float(0x7f800000);
-  lx = (n1.x - r.ox) * r.ix; hx = (n1.y - r.ox) * r.ix;
-  ly = (n1.z - r.oy) * r.iy; hy = (n1.w - r.oy) * r.iy;
-  lz = (n2.z - r.oz) * r.iz; hz = (n2.w - r.oz) * r.iz;
-  en = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fmaxf(fminf(lz, hz), r.tmin));
-  ex = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fmaxf(lz, hz)) * kRobustFar;
-  ex = fminf(ex, tbest);
-  t1 = en <= ex ? en : __int_as_float(0x7f800000);
+// Slack of the quantised slab test, 4 u (u = 2^-24).  The entry distance of a
+// quantised plane p + q 2^e is evaluated as fma(q, 2^e / d, (p - o) / d) with
+// (p - o) / d rounded twice; widening that last term by 4 u of its magnitude
+// (down for the near plane, up for the far one) bounds the rounding so that the
+// computed interval contains the exact one up to the relative factor that
+// kRobustFar absorbs, as in Ize's robust test.
+constexpr float kQuantSlack = 2.384185791015625e-07f;
+
+__device__ __forceinline__ float qbyte(uint32_t w, int shift) { return __uint2float_rn((w >> shift) & 0xffu); }
+
+// Tests the eight child boxes of wide node `node` (layout in bvh_build.h).  Out:
+// ng = (child_base, hit interior children at bits 24 + (slot ^ oct) | imask),
+// tg = (tri_base, hit triangles at their offsets from tri_base).
+__device__ __forceinline__ void wide_node(const SceneView &s, const RayPre &r, float tbest, uint32_t node,
+                                          uint2 &ng, uint2 &tg) {
+  const float4 *np = s.nodes + 5 * (size_t)node;
+  const float4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+  const uint32_t ei = __float_as_uint(w0.w);
+  const float ax = __fmul_rn(__uint_as_float((ei & 0xffu) << 23), r.ix);
+  const float ay = __fmul_rn(__uint_as_float(((ei >> 8) & 0xffu) << 23), r.iy);
+  const float az = __fmul_rn(__uint_as_float(((ei >> 16) & 0xffu) << 23), r.iz);
+  const float ox = __fmul_rn(__fsub_rn(w0.x, r.ox), r.ix);
+  const float oy = __fmul_rn(__fsub_rn(w0.y, r.oy), r.iy);
+  const float oz = __fmul_rn(__fsub_rn(w0.z, r.oz), r.iz);
+  const float nox = __fmaf_rn(-kQuantSlack, fabsf(ox), ox), fox = __fmaf_rn(kQuantSlack, fabsf(ox), ox);
+  const float noy = __fmaf_rn(-kQuantSlack, fabsf(oy), oy), foy = __fmaf_rn(kQuantSlack, fabsf(oy), oy);
+  const float noz = __fmaf_rn(-kQuantSlack, fabsf(oz), oz), foz = __fmaf_rn(kQuantSlack, fabsf(oz), oz);
+  // Near planes are the lo planes on axes the ray travels up, the hi planes otherwise.
+  const bool sx = r.ix < 0.f, sy = r.iy < 0.f, sz = r.iz < 0.f;
+  const uint32_t lx0 = __float_as_uint(w2.x), lx1 = __float_as_uint(w2.y);
+  const uint32_t hx0 = __float_as_uint(w2.z), hx1 = __float_as_uint(w2.w);
+  const uint32_t ly0 = __float_as_uint(w3.x), ly1 = __float_as_uint(w3.y);
+  const uint32_t hy0 = __float_as_uint(w3.z), hy1 = __float_as_uint(w3.w);
+  const uint32_t lz0 = __float_as_uint(w4.x), lz1 = __float_as_uint(w4.y);
+  const uint32_t hz0 = __float_as_uint(w4.z), hz1 = __float_as_uint(w4.w);
+  const uint32_t nx[2] = {sx ? hx0 : lx0, sx ? hx1 : lx1}, fx[2] = {sx ? lx0 : hx0, sx ? lx1 : hx1};
+  const uint32_t ny[2] = {sy ? hy0 : ly0, sy ? hy1 : ly1}, fy[2] = {sy ? ly0 : hy0, sy ? ly1 : hy1};
+  const uint32_t nz[2] = {sz ? hz0 : lz0, sz ? hz1 : lz1}, fz[2] = {sz ? lz0 : hz0, sz ? lz1 : hz1};
+  // Interior slots' meta bytes (0x38 + slot) become 0x38 + (slot ^ oct): their hit
+  // bit then orders the children front to back for the ray's octant.
+  const uint32_t x4 = r.oct * 0x01010101u;
+  uint32_t meta[2] = {__float_as_uint(w1.z), __float_as_uint(w1.w)};
+#pragma unroll
+  for (int h = 0; h < 2; ++h) meta[h] ^= (((meta[h] >> 3) & (meta[h] >> 4) & 0x01010101u) * 7u) & x4;
+  uint32_t hits = 0;
+#pragma unroll
+  for (int slot = 0; slot < 8; ++slot) {
+    const int h = slot >> 2, sh = (slot & 3) * 8;
+    const float tnx = __fmaf_rn(qbyte(nx[h], sh), ax, nox), tfx = __fmaf_rn(qbyte(fx[h], sh), ax, fox);
+    const float tny = __fmaf_rn(qbyte(ny[h], sh), ay, noy), tfy = __fmaf_rn(qbyte(fy[h], sh), ay, foy);
+    const float tnz = __fmaf_rn(qbyte(nz[h], sh), az, noz), tfz = __fmaf_rn(qbyte(fz[h], sh), az, foz);
+    const float en = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
+    const float ex = fminf(__fmul_rn(fminf(fminf(tfx, tfy), tfz), kRobustFar), tbest);
+    const uint32_t m = (meta[h] >> sh) & 0xffu;
+    if (en <= ex) hits |= (m >> 5) << (m & 31u);
+  }
+  ng = make_uint2(__float_as_uint(w1.x), (hits & 0xff000000u) | (ei >> 24));
+  tg = make_uint2(__float_as_uint(w1.y), hits & 0x00ffffffu);
 }
 
-// One traversal step of a ray: an interior node (both child boxes; the nearer hit
-// child next, the farther pushed) or a leaf (its triangles, then a pop).  `node` is
-// kDone when the ray is finished.  Stack as in trace_ray.
+// Traversal state of one ray: ng = the node group being expanded (child_base,
+// remaining interior-child hit bits | imask), tg = the triangles still to test
+// (tri_base, hit bits), sp = node groups on the stack.
+struct Trav {
+  uint2 ng, tg;
+  int sp;
+};
+
+// A pseudo group whose only hit bit selects node 0, the root.  A ray with a NaN
+// origin or direction can hit nothing (every triangle test fails) but would pass
+// every box test, so it does not enter the tree.
+__device__ __forceinline__ Trav trav_start(const SceneView &s, const RayPre &r) {
+  const bool ok = !isnan(r.ox + r.oy + r.oz + r.dx + r.dy + r.dz);
+  return Trav{make_uint2(0u, s.root == 0 && ok ? 0x80000000u : 0u), make_uint2(0u, 0u), 0};
+}
+
+// One traversal step: when no triangle is pending, visits the next node (the
+// group's highest-priority hit child; the rest of the group is pushed), then
+// tests one pending triangle.  The stack lives in shared memory, one column per
+// thread (stack[level * stride]), `depth` entries.  Returns false when the ray is
+// finished (ANY: at its first hit).
 template <bool ANY>
-__device__ __forceinline__ void trace_step(const SceneView &s, const RayPre &r, float &tbest, uint32_t &best,
-                                           int32_t &node, int &sp, int32_t *stack, int stride, int depth) {
-  if (node >= 0) {
-    const float4 *np = s.nodes + 4 * (size_t)node;
-    float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
-    float t0, t1;
-    hit_children(r, n0, n1, n2, tbest, t0, t1);
-    int32_t l0 = __float_as_int(n3.x), l1 = __float_as_int(n3.y);
-    bool h0 = t0 != __int_as_float(0x7f800000), h1 = t1 != __int_as_float(0x7f800000);
-    if (h0 && h1) {
-      int32_t near = l0, far = l1;
-      if (t1 < t0) { near = l1; far = l0; }
-      if (sp >= depth) {
-        atomicCAS(s.status, 0, -4 /* CKR_ERR_STACK_OVERFLOW */);
-        best = kMiss;
-        node = kDone;
-        return;
-      }
-      stack[sp * stride] = far;
-      ++sp;
-      node = near;
-    } else if (h0 | h1) {
-      node = h0 ? l0 : l1;
-    } else {
-      node = sp > 0 ? stack[--sp * stride] : kDone;
+__device__ __forceinline__ bool trace_step(const SceneView &s, const RayPre &r, float &tbest, uint32_t &best,
+                                           Trav &st, uint2 *stack, int stride, int depth) {
+  // One exit at the end: early returns for the any-hit case split the warp's
+  // control flow and cost more issue slots than the work they skip.
+  bool live = true;
+  if (st.tg.y == 0) {
+    if ((st.ng.y & 0xff000000u) == 0) {
+      if (st.sp == 0)
+        live = false;
+      else
+        st.ng = stack[--st.sp * stride];
     }
-    return;
+    if (live) {
+      const uint32_t bit = 31 - __clz(st.ng.y);
+      st.ng.y &= ~(1u << bit);
+      const uint32_t slot = (bit - 24) ^ r.oct;
+      const uint32_t child = st.ng.x + __popc(st.ng.y & ((1u << slot) - 1u) & 0xffu);
+      if (st.ng.y & 0xff000000u) {
+        if (st.sp < depth) {
+          stack[st.sp++ * stride] = st.ng;
+        } else {
+          atomicCAS(s.status, 0, -4 /* CKR_ERR_STACK_OVERFLOW */);
+          best = kMiss;
+          live = false;
+        }
+      }
+      if (live) wide_node(s, r, tbest, child, st.ng, st.tg);
+    }
   }
-  // Leaf: ~node = (first << 3) | (count - 1).
-  uint32_t code = ~(uint32_t)node;
-  uint32_t first = code >> 3, count = (code & 7u) + 1u;
-  const float4 *tp = s.tris + 3 * (size_t)first;
-  for (uint32_t k = 0; k < count; ++k) {
-    float4 v0 = __ldg(tp + 3 * k), v1 = __ldg(tp + 3 * k + 1), v2 = __ldg(tp + 3 * k + 2);
+  if (live && st.tg.y != 0) {
+    const uint32_t k = __ffs(st.tg.y) - 1;
+    st.tg.y &= st.tg.y - 1;
+    const float4 *tp = s.tris + 3 * (size_t)(st.tg.x + k);
+    const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
     float t;
     if (hit_triangle(r, v0, v1, v2, tbest, t)) {
       tbest = t;
       best = __float_as_uint(v0.w);
-      if (ANY) {
-        node = kDone;
-        return;
-      }
+      if (ANY) live = false;
     }
   }
-  node = sp > 0 ? stack[--sp * stride] : kDone;
+  return live;
 }
 
-// Traces one ray.  ANY: stop at the first hit.  The stack lives in shared
-// memory, one column per thread (stack[level * stride]), `depth` entries.
-// Returns the hit id (kMiss, triangle index, or kSphereBit | sphere index)
-// and updates tbest to the hit distance.
+// Spheres of the scene, tested before the triangles.  Returns false when ANY is
+// satisfied by a sphere.
 template <bool ANY>
-__device__ __forceinline__ uint32_t trace_ray(const SceneView &s, const RayPre &r, float &tbest,
-                                              int32_t *stack, int stride, int depth) {
-  uint32_t best = kMiss;
+__device__ __forceinline__ bool trace_spheres(const SceneView &s, const RayPre &r, float &tbest, uint32_t &best) {
   for (uint32_t k = 0; k < s.nsph; ++k) {
     double t = hit_sphere(r, __ldg(&s.spheres[k]));
     if (t < (double)tbest) {
       tbest = (float)t;
       best = kSphereBit | k;
-      if (ANY) return best;
+      if (ANY) return false;
     }
   }
-  int32_t node = s.root;
-  int sp = 0;
-  while (node != kDone) {
-    if (node >= 0) {
-      const float4 *np = s.nodes + 4 * (size_t)node;
-      float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
-      float t0, t1;
-      hit_children(r, n0, n1, n2, tbest, t0, t1);
-      int32_t l0 = __float_as_int(n3.x), l1 = __float_as_int(n3.y);
-      bool h0 = t0 != __int_as_float(0x7f800000), h1 = t1 != __int_as_float(0x7f800000);
-      if (h0 && h1) {
-        int32_t near = l0, far = l1;
-        if (t1 < t0) { near = l1; far = l0; }
-        if (sp >= depth) {
-          atomicCAS(s.status, 0, -4 /* CKR_ERR_STACK_OVERFLOW */);
-          return kMiss;
-        }
-        stack[sp * stride] = far;
-        ++sp;
-        node = near;
-      } else if (h0 | h1) {
-        node = h0 ? l0 : l1;
-      } else {
-        node = sp > 0 ? stack[--sp * stride] : kDone;
-      }
-      continue;
-    }
-    // Leaf: ~node = (first << 3) | (count - 1).
-    uint32_t code = ~(uint32_t)node;
-    uint32_t first = code >> 3, count = (code & 7u) + 1u;
-    const float4 *tp = s.tris + 3 * (size_t)first;
-    for (uint32_t k = 0; k < count; ++k) {
-      float4 v0 = __ldg(tp + 3 * k), v1 = __ldg(tp + 3 * k + 1), v2 = __ldg(tp + 3 * k + 2);
-      float t;
-      if (hit_triangle(r, v0, v1, v2, tbest, t)) {
-        tbest = t;
-        best = __float_as_uint(v0.w);
-        if (ANY) return best;
-      }
-    }
-    node = sp > 0 ? stack[--sp * stride] : kDone;
+  return true;
+}
+
+// Traces one ray.  ANY: stop at the first hit.  Returns the hit id (kMiss,
+// triangle index, or kSphereBit | sphere index) and updates tbest to the hit
+// distance.
+template <bool ANY>
+__device__ __forceinline__ uint32_t trace_ray(const SceneView &s, const RayPre &r, float &tbest, uint2 *stack,
+                                              int stride, int depth) {
+  uint32_t best = kMiss;
+  if (!trace_spheres<ANY>(s, r, tbest, best)) return best;
+  Trav st = trav_start(s, r);
+  while (trace_step<ANY>(s, r, tbest, best, st, stack, stride, depth)) {
   }
   return best;
 }

@@ -1,8 +1,9 @@
 // trace_stats.cpp — host replay of the device traversal (closest-hit mode) that
-// counts child boxes and triangles tested per ray.  The counts define the
+// counts the wide nodes and triangles visited per ray.  The counts define the
 // algorithmic bytes per ray of the traversal roofline:
-//   bytes/ray = 32 (ray) + 8 (id + t) + boxes * 32 + triangles * 36.
-// The arithmetic mirrors trace_device.cuh (FP32, the same fused operations).
+//   bytes/ray = 32 (ray) + 8 (id + t) + nodes * 80 + triangles * 36.
+// The arithmetic and the visiting order mirror trace_device.cuh (FP32, the same
+// fused operations), so the replay reports the device's hits as well.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -13,7 +14,7 @@
 #include "bvh_build.h"
 
 namespace ckr {
-void scene_host_arrays(const ckr_scene *s, const float **nodes, const float **tris, const float **spheres,
+void scene_host_arrays(const ckr_scene *s, const uint32_t **nodes, const float **tris, const float **spheres,
                        int32_t *root, uint32_t *nsph, uint32_t *depth);
 }
 
@@ -25,6 +26,7 @@ constexpr float kRobustFar = 1.0000003576278687f;
 struct Pre {
   float o[3], d[3], inv[3], tmin;
   float mx[3], my[3], mz[3];
+  uint32_t oct;
 };
 
 Pre make_pre(const ckr_ray &ray) {
@@ -32,7 +34,10 @@ Pre make_pre(const ckr_ray &ray) {
   r.o[0] = ray.ox; r.o[1] = ray.oy; r.o[2] = ray.oz;
   r.d[0] = ray.dx; r.d[1] = ray.dy; r.d[2] = ray.dz;
   r.tmin = ray.tmin;
-  for (int k = 0; k < 3; ++k) r.inv[k] = 1.0f / r.d[k];
+  for (int k = 0; k < 3; ++k) {
+    float i = 1.0f / r.d[k];
+    r.inv[k] = std::fabs(i) > 1e20f ? std::copysign(1e20f, i) : i;  // kMaxInvDir of trace_device.cuh
+  }
   float ax = std::fabs(r.d[0]), ay = std::fabs(r.d[1]), az = std::fabs(r.d[2]);
   int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
   int kx = kz == 2 ? 0 : kz + 1;
@@ -44,6 +49,7 @@ Pre make_pre(const ckr_ray &ray) {
     r.my[k] = (ky == k) ? 1.f : (kz == k ? -sy : 0.f);
     r.mz[k] = (kz == k) ? sz : 0.f;
   }
+  r.oct = 7u ^ ((r.d[0] < 0.f ? 4u : 0u) | (r.d[1] < 0.f ? 2u : 0u) | (r.d[2] < 0.f ? 1u : 0u));
   return r;
 }
 
@@ -83,64 +89,86 @@ bool hit_tri(const Pre &r, const float *t12, float tbest, float &tout) {
   return true;
 }
 
-float child_entry(const Pre &r, float lx_, float hx_, float ly_, float hy_, float lz_, float hz_, float tbest) {
-  float lx = (lx_ - r.o[0]) * r.inv[0], hx = (hx_ - r.o[0]) * r.inv[0];
-  float ly = (ly_ - r.o[1]) * r.inv[1], hy = (hy_ - r.o[1]) * r.inv[1];
-  float lz = (lz_ - r.o[2]) * r.inv[2], hz = (hz_ - r.o[2]) * r.inv[2];
-  float en = std::fmax(std::fmax(std::fmin(lx, hx), std::fmin(ly, hy)), std::fmax(std::fmin(lz, hz), r.tmin));
-  float ex = std::fmin(std::fmin(std::fmax(lx, hx), std::fmax(ly, hy)), std::fmax(lz, hz)) * kRobustFar;
-  ex = std::fmin(ex, tbest);
-  return en <= ex ? en : INFINITY;
+constexpr float kQuantSlack = 2.384185791015625e-07f;
+
+inline float f_of(uint32_t w) {
+  float f;
+  std::memcpy(&f, &w, 4);
+  return f;
 }
 
-uint32_t replay(const float *nodes, const float *tris, int32_t root, const ckr_ray &ray, uint64_t &boxes,
-                uint64_t &ntris, float &tbest) {
+// wide_node of trace_device.cuh.
+void wide_node(const uint32_t *w, const Pre &r, float tbest, uint32_t ng[2], uint32_t tg[2]) {
+  float adj[3], on[3], of[3];
+  for (int a = 0; a < 3; ++a) {
+    float scale = f_of(((w[3] >> (8 * a)) & 0xffu) << 23);
+    adj[a] = scale * r.inv[a];
+    float o = (f_of(w[a]) - r.o[a]) * r.inv[a];
+    on[a] = std::fma(-kQuantSlack, std::fabs(o), o);
+    of[a] = std::fma(kQuantSlack, std::fabs(o), o);
+  }
+  uint32_t meta[2] = {w[6], w[7]};
+  const uint32_t x4 = r.oct * 0x01010101u;
+  for (int h = 0; h < 2; ++h) meta[h] ^= (((meta[h] >> 3) & (meta[h] >> 4) & 0x01010101u) * 7u) & x4;
+  uint32_t hits = 0;
+  for (int slot = 0; slot < 8; ++slot) {
+    const int h = slot >> 2, sh = (slot & 3) * 8;
+    float tn[3], tf[3];
+    for (int a = 0; a < 3; ++a) {
+      const bool neg = r.inv[a] < 0.f;
+      const uint32_t lo = w[8 + 4 * a + h], hi = w[10 + 4 * a + h];
+      const float qn = (float)(((neg ? hi : lo) >> sh) & 0xffu), qf = (float)(((neg ? lo : hi) >> sh) & 0xffu);
+      tn[a] = std::fma(qn, adj[a], on[a]);
+      tf[a] = std::fma(qf, adj[a], of[a]);
+    }
+    const float en = std::fmax(std::fmax(tn[0], tn[1]), std::fmax(tn[2], r.tmin));
+    const float ex = std::fmin(std::fmin(std::fmin(tf[0], tf[1]), tf[2]) * kRobustFar, tbest);
+    const uint32_t m = (meta[h] >> sh) & 0xffu;
+    if (en <= ex) hits |= (m >> 5) << (m & 31u);
+  }
+  ng[0] = w[4];
+  ng[1] = (hits & 0xff000000u) | (w[3] >> 24);
+  tg[0] = w[5];
+  tg[1] = hits & 0x00ffffffu;
+}
+
+inline int highest_bit(uint32_t x) { return 31 - __builtin_clz(x); }
+
+uint32_t replay(const uint32_t *nodes, const float *tris, int32_t root, const ckr_ray &ray, uint64_t &nnodes,
+                uint64_t &ntris, float &tbest, bool any = false) {
   Pre r = make_pre(ray);
   tbest = ray.tmax;
   uint32_t best = 0xFFFFFFFFu;
-  std::vector<int32_t> stack;
-  int32_t node = root;
-  while (node != kDone) {
-    if (node >= 0) {
-      const float *n = nodes + 16 * (size_t)node;
-      boxes += 2;
-      float t0 = child_entry(r, n[0], n[1], n[2], n[3], n[8], n[9], tbest);
-      float t1 = child_entry(r, n[4], n[5], n[6], n[7], n[10], n[11], tbest);
-      int32_t l0, l1;
-      std::memcpy(&l0, &n[12], 4);
-      std::memcpy(&l1, &n[13], 4);
-      bool h0 = t0 != INFINITY, h1 = t1 != INFINITY;
-      if (h0 && h1) {
-        int32_t near = l0, far = l1;
-        if (t1 < t0) std::swap(near, far);
-        stack.push_back(far);
-        node = near;
-      } else if (h0 || h1) {
-        node = h0 ? l0 : l1;
-      } else if (!stack.empty()) {
-        node = stack.back();
+  std::vector<std::pair<uint32_t, uint32_t>> stack;
+  const bool ok = !std::isnan(r.o[0] + r.o[1] + r.o[2] + r.d[0] + r.d[1] + r.d[2]);
+  uint32_t ng[2] = {0u, root == 0 && ok ? 0x80000000u : 0u}, tg[2] = {0u, 0u};
+  for (;;) {
+    if (tg[1] == 0) {
+      if ((ng[1] & 0xff000000u) == 0) {
+        if (stack.empty()) break;
+        ng[0] = stack.back().first;
+        ng[1] = stack.back().second;
         stack.pop_back();
-      } else {
-        node = kDone;
       }
-      continue;
+      const int bit = highest_bit(ng[1]);
+      ng[1] &= ~(1u << bit);
+      const uint32_t slot = (uint32_t)(bit - 24) ^ r.oct;
+      const uint32_t child = ng[0] + (uint32_t)__builtin_popcount(ng[1] & ((1u << slot) - 1u) & 0xffu);
+      if (ng[1] & 0xff000000u) stack.push_back({ng[0], ng[1]});
+      nnodes++;
+      wide_node(nodes + (size_t)child * ckr::kWideWords, r, tbest, ng, tg);
     }
-    uint32_t code = ~(uint32_t)node;
-    uint32_t first = code >> 3, count = (code & 7u) + 1u;
-    for (uint32_t k = 0; k < count; ++k) {
+    if (tg[1] != 0) {
+      const uint32_t k = (uint32_t)__builtin_ctz(tg[1]);
+      tg[1] &= tg[1] - 1;
       ntris++;
       float t;
-      const float *tp = tris + 12 * (size_t)(first + k);
+      const float *tp = tris + 12 * (size_t)(tg[0] + k);
       if (hit_tri(r, tp, tbest, t)) {
         tbest = t;
         std::memcpy(&best, &tp[3], 4);
+        if (any) break;
       }
-    }
-    if (!stack.empty()) {
-      node = stack.back();
-      stack.pop_back();
-    } else {
-      node = kDone;
     }
   }
   return best;
@@ -148,10 +176,11 @@ uint32_t replay(const float *nodes, const float *tris, int32_t root, const ckr_r
 
 }  // namespace
 
-extern "C" int ckr_trace_stats(const ckr_scene *scene, const ckr_ray *rays, uint32_t n, double *mean_boxes,
+extern "C" int ckr_trace_stats(const ckr_scene *scene, const ckr_ray *rays, uint32_t n, double *mean_nodes,
                                double *mean_tris) {
-  if (!scene || (n && !rays) || !mean_boxes || !mean_tris) return CKR_ERR_INVALID_ARGUMENT;
-  const float *nodes, *tris, *spheres;
+  if (!scene || (n && !rays) || !mean_nodes || !mean_tris) return CKR_ERR_INVALID_ARGUMENT;
+  const uint32_t *nodes;
+  const float *tris, *spheres;
   int32_t root;
   uint32_t nsph, depth;
   ckr::scene_host_arrays(scene, &nodes, &tris, &spheres, &root, &nsph, &depth);
@@ -169,18 +198,19 @@ extern "C" int ckr_trace_stats(const ckr_scene *scene, const ckr_ray *rays, uint
     B += bx[w];
     T += tr[w];
   }
-  *mean_boxes = n ? (double)B / n : 0.0;
+  *mean_nodes = n ? (double)B / n : 0.0;
   *mean_tris = n ? (double)T / n : 0.0;
   return CKR_OK;
 }
 
-// Host-only replay of the whole closest-hit path (SAH build + FP32 traversal)
+// Host-only replay of the whole closest-hit (any = 0) or any-hit path (SAH build +
+// FP32 traversal)
 // without a device, for the CPU test suite: it lets the builder and the
 // traversal logic be checked against the oracle before any kernel runs.  Not
 // part of the public ABI and not used by any product entry point.
-extern "C" int ckr_internal_replay_closest(const float *tri9, uint32_t ntri, uint32_t max_leaf,
-                                           const ckr_ray *rays, uint32_t n, uint32_t *hit_id, float *hit_t,
-                                           double *mean_boxes, double *mean_tris) {
+extern "C" int ckr_internal_replay(const float *tri9, uint32_t ntri, uint32_t max_leaf, const ckr_ray *rays,
+                                   uint32_t n, int any, uint32_t *hit_id, float *hit_t, double *mean_nodes,
+                                   double *mean_tris) {
   ckr::FlatBvh bvh;
   ckr_build_params p{max_leaf, 0, 0};
   int st = ckr::build_bvh(tri9, ntri, p, bvh);
@@ -188,10 +218,10 @@ extern "C" int ckr_internal_replay_closest(const float *tri9, uint32_t ntri, uin
   uint64_t B = 0, T = 0;
   for (uint32_t i = 0; i < n; ++i) {
     float t;
-    hit_id[i] = replay(bvh.nodes.data(), bvh.tris.data(), bvh.root, rays[i], B, T, t);
+    hit_id[i] = replay(bvh.nodes.data(), bvh.tris.data(), bvh.root, rays[i], B, T, t, any != 0);
     hit_t[i] = t;
   }
-  if (mean_boxes) *mean_boxes = n ? (double)B / n : 0.0;
+  if (mean_nodes) *mean_nodes = n ? (double)B / n : 0.0;
   if (mean_tris) *mean_tris = n ? (double)T / n : 0.0;
   return CKR_OK;
 }

@@ -180,8 +180,8 @@ __global__ void __launch_bounds__(TPB) k_camera(Cam cam0, Paths P, Params prm, u
 
 template <int TPB>
 __global__ void __launch_bounds__(TPB) k_extend(SceneView s, Paths P, int cur, int depth) {
-  extern __shared__ int32_t smem_stack[];
-  int32_t *stack = smem_stack + threadIdx.x;
+  extern __shared__ uint2 smem_trav[];
+  uint2 *stack = smem_trav + threadIdx.x;
   const uint32_t n = P.counts[cur];
   const uint32_t *q = cur ? P.q1 : P.q0;
   for (uint32_t i = blockIdx.x * TPB + threadIdx.x; i < n; i += gridDim.x * TPB) {
@@ -198,8 +198,8 @@ __global__ void __launch_bounds__(TPB) k_extend(SceneView s, Paths P, int cur, i
 
 template <int TPB>
 __global__ void __launch_bounds__(TPB) k_shadow(SceneView s, Paths P, int depth, int cur, float4 *rec) {
-  extern __shared__ int32_t smem_stack[];
-  int32_t *stack = smem_stack + threadIdx.x;
+  extern __shared__ uint2 smem_trav[];
+  uint2 *stack = smem_trav + threadIdx.x;
   const uint32_t n = P.counts[2];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     // Ray statistics: closest-hit rays of this bounce and its shadow rays.
@@ -523,7 +523,7 @@ __global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params pr
     // direction, redrawn while it meets an emitter (emitters only count through the
     // direct term), traced here; beta *= c 2 pi cos f / 0.7.
     if (SHADER == CKR_SHADER_EXPLICIT) {
-      extern __shared__ int32_t smem_stack[];
+      extern __shared__ uint2 smem_trav[];
       uint32_t hit = kMiss;
       float th = 0.f;
       F3 wn = f3(0, 0, 0);
@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params pr
                                  ckr_draw_f(key, ctr(meta.y, meta.z, kDimHemi + 2 * r + 1)));
           RayPre rp = ray_pre(o_off, wn, 0.f);
           th = 3.0e38f;
-          hit = trace_ray<false>(scene, rp, th, smem_stack + threadIdx.x, TPB, stack_depth);
+          hit = trace_ray<false>(scene, rp, th, smem_trav + threadIdx.x, TPB, stack_depth);
           if (hit == kMiss) {
             done = true;  // escapes the scene
           } else {

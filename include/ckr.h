@@ -68,10 +68,10 @@ typedef struct ckr_build_params {
 
 typedef struct ckr_scene_info {
   uint32_t ntri, nsph;
-  uint32_t nnodes;     /* interior nodes (each holds two child boxes) */
-  uint32_t nleaves;
-  uint32_t max_depth;  /* = traversal stack entries needed */
-  uint32_t reserved;
+  uint32_t nnodes;     /* wide nodes (each holds up to eight child boxes) */
+  uint32_t nleaves;    /* leaf children (runs of 1..3 triangles) */
+  uint32_t max_depth;  /* levels of wide nodes = traversal stack entries needed */
+  uint32_t nnodes_binary; /* interior nodes of the binary SAH tree before collapsing */
   uint64_t device_bytes;
   double build_ms;
 } ckr_scene_info;
@@ -119,11 +119,12 @@ int ckr_trace_closest_host(ckr_scene *scene, const ckr_ray *rays, uint32_t n,
 int ckr_trace_any_host(ckr_scene *scene, const ckr_ray *rays, uint32_t n,
                        uint8_t *occluded, void *stream);
 
-/* Host replay of the device traversal in the same FP32 arithmetic: mean child
- * boxes tested and triangles tested per ray (closest-hit mode), used for the
- * algorithmic-bytes roofline.  rays are host memory. */
+/* Host replay of the device traversal in the same FP32 arithmetic: mean wide
+ * nodes visited (80 bytes each, eight child boxes) and triangles tested per ray
+ * (closest-hit mode), used for the algorithmic-bytes roofline.  rays are host
+ * memory. */
 int ckr_trace_stats(const ckr_scene *scene, const ckr_ray *rays, uint32_t n,
-                    double *mean_boxes, double *mean_tris);
+                    double *mean_nodes, double *mean_tris);
 
 /* ---- full scenes: materials, lights, rendering --------------------------- */
 /* MaterialType + BasePrimitive colour/reflectance (headers/materialTypes.h:21-98,

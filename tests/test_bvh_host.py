@@ -17,10 +17,10 @@ from parity import classify
 GOLD = Path(__file__).resolve().parent / "golden"
 
 
-def replay(tri, rays, leaf=4):
+def replay(tri, rays, leaf=4, any_hit=False):
     L = ckr.lib()
-    f = L.ckr_internal_replay_closest
-    f.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
+    f = L.ckr_internal_replay
+    f.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p, C.c_void_p,
                   C.POINTER(C.c_double), C.POINTER(C.c_double)]
     f.restype = C.c_int
     tri = np.ascontiguousarray(tri, dtype=np.float32)
@@ -28,8 +28,8 @@ def replay(tri, rays, leaf=4):
     ids = np.empty(len(rays), dtype=np.uint32)
     t = np.empty(len(rays), dtype=np.float32)
     b, n = C.c_double(), C.c_double()
-    st = f(tri.ctypes.data if len(tri) else None, len(tri), leaf, rays.ctypes.data, len(rays), ids.ctypes.data,
-           t.ctypes.data, C.byref(b), C.byref(n))
+    st = f(tri.ctypes.data if len(tri) else None, len(tri), leaf, rays.ctypes.data, len(rays), int(any_hit),
+           ids.ctypes.data, t.ctypes.data, C.byref(b), C.byref(n))
     assert st == 0, st
     return ids, t, b.value, n.value
 
@@ -56,13 +56,14 @@ def test_replay_medium_mesh_vs_oracle():
     lo, hi = tri.reshape(-1, 3).min(0), tri.reshape(-1, 3).max(0)
     rays = np.concatenate([ckr.rays_pinhole([0, 0, 3], [0, 0, 0], [0, 1, 0], 40.0, 96, 96),
                            ckr.rays_incoherent(lo, hi, 7, 8192)])
-    ids, t, boxes, ntris = replay(tri, rays)
+    ids, t, nodes, ntris = replay(tri, rays)
     oid, ot = O.OracleBvh(tri).closest(rays)
     c = classify(tri, rays, ids, t, oid, ot)
     assert not c["bad"], c
     assert c["edge"] <= 3
-    # An SAH tree visits far fewer boxes than the reference's midpoint tree (~130 nodes/ray).
-    assert boxes < 100 and ntris < 12
+    # The reference's midpoint tree visits ~130 binary nodes per ray; the collapsed SAH
+    # tree visits about 9 eight-wide nodes (measured 9.4) and 3.6 triangles.
+    assert nodes < 14 and ntris < 6
 
 
 def test_degenerate_inputs_build():

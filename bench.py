@@ -476,7 +476,31 @@ def case_manylight_split():
     torch.cuda.synchronize()
 
 
-CASES = {"manylight-learned": case_manylight_learned, "manylight-split": case_manylight_split}
+def case_trace():
+    """The traversal workload (2^23 rays over the 1.3M-triangle icosphere, 0.4 GB on
+    the device) for profilers: two closest-hit launches, then two any-hit launches."""
+    import torch
+    from chakumrender_gb300 import build
+    from chakumrender_gb300 import ckr
+
+    build.build_library()
+    tri, closest, anyhit = make_workload()
+    scene = ckr.Scene(tri)
+    n = len(closest)
+    s = torch.cuda.current_stream().cuda_stream
+    d_rays, d_any = torch.from_numpy(closest).cuda(), torch.from_numpy(anyhit).cuda()
+    ids = torch.empty(n, dtype=torch.int32, device="cuda")
+    ts = torch.empty(n, dtype=torch.float32, device="cuda")
+    occ = torch.empty(n, dtype=torch.uint8, device="cuda")
+    for _ in range(2):
+        scene.trace_closest(d_rays.data_ptr(), n, ids.data_ptr(), ts.data_ptr(), s)
+    for _ in range(2):
+        scene.trace_any(d_any.data_ptr(), n, occ.data_ptr(), s)
+    if scene.check_device(s) != 0:
+        raise SystemExit("device status error")
+
+
+CASES = {"manylight-learned": case_manylight_learned, "manylight-split": case_manylight_split, "trace": case_trace}
 
 
 def main():
@@ -485,7 +509,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--leaf", type=int, default=4)
+    ap.add_argument("--leaf", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--case", default=None, choices=sorted(CASES),
                     help="run one small workload and exit (for profiling; prints nothing to parse)")
@@ -604,8 +628,9 @@ def main():
         "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "rays_per_step": n, "triangles": int(info.ntri),
-                   "bvh": (f"binned SAH, leaf<={args.leaf} ({info.nnodes_binary} binary nodes), collapsed to "
-                           f"8-wide, 8-bit quantised boxes: {info.nnodes} wide nodes, depth {info.max_depth}"),
+                   "bvh": (f"binned SAH to single triangles ({info.nnodes_binary} binary nodes), SAH-optimal "
+                           f"collapse to 8-wide nodes with 8-bit quantised boxes and leaves <= {min(args.leaf, 3)}: "
+                           f"{info.nnodes} wide nodes, depth {info.max_depth}"),
                    "bvh_build_ms": round(info.build_ms, 1), "l2": "inputs larger than L2 (rays 256 MiB), no flush",
                    "parallelism": f"replica x{world}"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",

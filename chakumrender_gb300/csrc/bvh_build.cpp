@@ -182,39 +182,113 @@ struct Builder {
 inline double plane(float p, uint32_t q, int e) { return (double)p + std::ldexp((double)q, e); }
 
 // One child of a wide node under construction: an interior node of the binary
-// tree, or a run of at most kWideLeafMax triangles of one of its leaves.
+// tree that becomes a wide node, or a leaf of 1..3 triangles.
 struct Entry {
   Box box;
   uint32_t tnode;         // interior: binary-tree node
   uint32_t begin, count;  // leaf: prims[begin, begin + count); count 0 for interior
 };
 
-void entries_of(const Builder &b, uint32_t ti, std::vector<Entry> &out) {
-  const TNode &n = b.pool[ti];
-  if (n.count == 0) {
-    out.push_back({n.box, ti, 0, 0});
-    return;
-  }
-  for (uint32_t i = n.begin; i < n.begin + n.count; i += kWideLeafMax) {
-    Entry e{};
-    e.count = std::min(kWideLeafMax, n.begin + n.count - i);
-    e.begin = i;
-    e.box.reset();
-    for (uint32_t k = i; k < i + e.count; ++k) e.box.grow(b.prims[k].box);
-    out.push_back(e);
+// SAH cost model of the collapse: a wide-node visit costs kCostNode, a triangle
+// test kCostPrim, each weighted by the surface area of the box whose hit leads to
+// it.  A triangle test takes about a third of the instructions of a node visit,
+// but the traversal tests one triangle per step while lanes of the warp visit
+// nodes, so on the device it costs about as much as a visit: sweeping kCostPrim
+// over 0.3 .. 1.5 on the 1.3M-triangle workload, 0.3 was 5 % slower and 1.0 .. 1.5
+// equal.
+constexpr float kCostNode = 1.0f, kCostPrim = 1.0f;
+
+// Optimal collapse of the binary tree (the dynamic programme of Ylitie et al.
+// 2017).  For binary node n, cost[8n + j - 1] is the least cost of spreading n's
+// subtree over at most j slots of the wide node above it: n itself in one slot
+// (as a leaf of <= leaf_max triangles or as a wide node of its own), or the
+// slots shared between its two children.
+struct Plan {
+  std::vector<float> cost;
+  std::vector<uint8_t> split;   // per (n, j): 0 = n takes one slot, k = k slots to the left child
+  std::vector<uint8_t> leaf;    // n in one slot is a leaf (else a wide node)
+  std::vector<uint8_t> wsplit;  // n as a wide node: slots of its left child (right: 8 - wsplit)
+  std::vector<uint32_t> begin, count;  // n's triangles: prims[begin, begin + count)
+};
+
+void make_plan(const Builder &b, uint32_t leaf_max, Plan &p) {
+  const uint32_t N = b.next.load();
+  p.cost.assign((size_t)N * 8, 0.f);
+  p.split.assign((size_t)N * 8, 0);
+  p.leaf.assign(N, 0);
+  p.wsplit.assign(N, 1);
+  p.begin.assign(N, 0);
+  p.count.assign(N, 0);
+  // Children are allocated after their parent: reverse index order is bottom-up.
+  for (uint32_t i = N; i-- > 0;) {
+    const TNode &n = b.pool[i];
+    float *d = &p.cost[(size_t)i * 8];
+    const float area = n.box.area();
+    if (n.count) {  // binary leaf (one triangle: the binary tree is built with leaf size 1)
+      p.begin[i] = n.begin;
+      p.count[i] = n.count;
+      p.leaf[i] = 1;
+      for (int j = 0; j < 8; ++j) d[j] = area * (float)n.count * kCostPrim;
+      continue;
+    }
+    const uint32_t L = n.left, R = L + 1;
+    p.begin[i] = p.begin[L];
+    p.count[i] = p.count[L] + p.count[R];
+    const float *dl = &p.cost[(size_t)L * 8], *dr = &p.cost[(size_t)R * 8];
+    float best = std::numeric_limits<float>::infinity();
+    int bk = 1;
+    for (int k = 1; k <= 7; ++k) {
+      const float c = dl[k - 1] + dr[8 - k - 1];
+      if (c < best) {
+        best = c;
+        bk = k;
+      }
+    }
+    const float c_wide = area * kCostNode + best;
+    const float c_leaf = p.count[i] <= leaf_max ? area * (float)p.count[i] * kCostPrim
+                                                : std::numeric_limits<float>::infinity();
+    const float c1 = std::min(c_leaf, c_wide);
+    p.leaf[i] = c_leaf <= c_wide;
+    p.wsplit[i] = (uint8_t)bk;
+    d[0] = c1;
+    for (int j = 2; j <= 8; ++j) {
+      float bj = c1;
+      int sj = 0;
+      for (int k = 1; k < j; ++k) {
+        const float c = dl[k - 1] + dr[j - k - 1];
+        if (c < bj) {
+          bj = c;
+          sj = k;
+        }
+      }
+      d[j - 1] = bj;
+      p.split[(size_t)i * 8 + j - 1] = (uint8_t)sj;
+    }
   }
 }
 
-uint32_t slots_of(const TNode &n) { return n.count ? (n.count + kWideLeafMax - 1) / kWideLeafMax : 1; }
+// The slot children of binary node n spread over at most j slots.
+void gather(const Builder &b, const Plan &p, uint32_t n, uint32_t j, std::vector<Entry> &out) {
+  const uint32_t s = p.split[(size_t)n * 8 + j - 1];
+  if (s == 0) {
+    if (p.leaf[n])
+      out.push_back({b.pool[n].box, 0, p.begin[n], p.count[n]});
+    else
+      out.push_back({b.pool[n].box, n, 0, 0});
+    return;
+  }
+  gather(b, p, b.pool[n].left, s, out);
+  gather(b, p, b.pool[n].left + 1, j - s, out);
+}
 
-// Collapses the binary tree into wide nodes.  Each wide node starts from the two
-// children of a binary node and repeatedly opens the child with the largest
-// surface area while the children still fit in eight slots.  Children go to
+// Collapses the binary tree into wide nodes following the plan.  Children go to
 // slots by a greedy assignment on cost(child, slot) = (centroid - node centre) .
 // dir(slot), dir = the octant's signs, so that slot o holds the child nearest the
 // start of rays travelling in octant o.  Boxes are quantised outward.
-void collapse(const Builder &b, const float *tri9, FlatBvh &out) {
+void collapse(const Builder &b, const float *tri9, uint32_t leaf_max, FlatBvh &out) {
   const uint32_t n = (uint32_t)b.prims.size();
+  Plan plan;
+  make_plan(b, leaf_max, plan);
   out.tris.reserve((size_t)n * 12);
   out.nnodes_binary = 0;
   for (uint32_t i = 0; i < (uint32_t)b.next.load(); ++i)
@@ -233,29 +307,10 @@ void collapse(const Builder &b, const float *tri9, FlatBvh &out) {
     const TNode &tn = b.pool[wk.tnode];
     kids.clear();
     if (tn.count > 0) {
-      entries_of(b, wk.tnode, kids);  // the whole tree is one leaf
+      kids.push_back({tn.box, 0, tn.begin, tn.count});  // the whole tree is one triangle
     } else {
-      entries_of(b, tn.left, kids);
-      entries_of(b, tn.left + 1, kids);
-    }
-    for (;;) {
-      int best = -1;
-      float best_area = -1.f;
-      for (size_t k = 0; k < kids.size(); ++k) {
-        if (kids[k].count) continue;
-        const TNode &c = b.pool[kids[k].tnode];
-        uint32_t need = (uint32_t)kids.size() - 1 + slots_of(b.pool[c.left]) + slots_of(b.pool[c.left + 1]);
-        float area = c.box.area();
-        if (need <= 8 && area > best_area) {
-          best_area = area;
-          best = (int)k;
-        }
-      }
-      if (best < 0) break;
-      uint32_t ti = kids[best].tnode;
-      kids.erase(kids.begin() + best);
-      entries_of(b, b.pool[ti].left, kids);
-      entries_of(b, b.pool[ti].left + 1, kids);
+      gather(b, plan, tn.left, plan.wsplit[wk.tnode], kids);
+      gather(b, plan, tn.left + 1, 8 - plan.wsplit[wk.tnode], kids);
     }
     // Node box and quantisation grid.
     Box nb;
@@ -353,9 +408,13 @@ void collapse(const Builder &b, const float *tri9, FlatBvh &out) {
 int build_bvh(const float *tri9, uint32_t ntri, const ckr_build_params &params, FlatBvh &out) {
   out = FlatBvh();
   Builder b;
-  b.max_leaf = params.max_leaf_size ? params.max_leaf_size : 4;
+  // The binary tree splits down to single triangles; the collapse chooses the
+  // wide tree's leaves (at most leaf_max <= kWideLeafMax triangles each).
+  const uint32_t req = params.max_leaf_size ? params.max_leaf_size : kWideLeafMax;
   b.bins = params.sah_bins ? params.sah_bins : 16;
-  if (b.max_leaf < 1 || b.max_leaf > 8 || b.bins < 4 || b.bins > 64) return CKR_ERR_INVALID_ARGUMENT;
+  if (req < 1 || req > 8 || b.bins < 4 || b.bins > 64) return CKR_ERR_INVALID_ARGUMENT;
+  const uint32_t leaf_max = std::min(req, kWideLeafMax);
+  b.max_leaf = 1;
   unsigned hw = std::thread::hardware_concurrency();
   uint32_t threads = params.threads ? params.threads : (hw ? hw : 1);
   b.spare_threads = (int)threads - 1;
@@ -387,7 +446,7 @@ int build_bvh(const float *tri9, uint32_t ntri, const ckr_build_params &params, 
   for (const Prim &p : b.prims) b.pool[0].box.grow(p.box);
   b.build(0, 0, n);
 
-  collapse(b, tri9, out);
+  collapse(b, tri9, leaf_max, out);
   return validate_bvh(out) ? CKR_OK : CKR_ERR_INVALID_ARGUMENT;
 }
 

@@ -81,8 +81,13 @@ struct ckr_scene {
   ckr::DevBuf<uint32_t> st_id;
   ckr::DevBuf<float> st_t;
   ckr::DevBuf<uint8_t> st_occ;
-  cudaStream_t pipe[2] = {nullptr, nullptr};
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  ckr::DevBuf<uint32_t> st_next;  // ray counters of the pipeline streams
+  int trace_grid[2] = {1, 1};     // persistent grids of the closest / any-hit kernels
+  size_t trace_smem = 0;          // their traversal stacks
+  static constexpr int kMaxPipes = 4;
+  cudaStream_t pipe[kMaxPipes] = {};
+  cudaEvent_t pipe_done[kMaxPipes] = {};
+  cudaEvent_t user_ready = nullptr;
 };
 
 namespace ckr {

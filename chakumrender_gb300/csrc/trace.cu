@@ -99,8 +99,10 @@ struct LaunchShape {
   size_t smem;
 };
 
+// Persistent grid of the traversal kernel for scene s: as many blocks as fit on
+// the device at once.
 template <bool ANY>
-cudaError_t launch_shape(const ckr_scene *s, uint32_t n, LaunchShape &ls) {
+cudaError_t launch_shape(const ckr_scene *s, LaunchShape &ls) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
@@ -114,36 +116,39 @@ cudaError_t launch_shape(const ckr_scene *s, uint32_t n, LaunchShape &ls) {
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_dyn<ANY>, kTPB, ls.smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  int want = (int)ceil_div(n, kTPB);
-  ls.grid = std::max(1, std::min(want, sms * per_sm));
+  ls.grid = sms * per_sm;
   return cudaSuccess;
 }
 
+// Launches the traversal of rays[0, n).  `next` is a zeroed-per-launch ray counter
+// owned by the caller (one per concurrently used stream), or null to allocate one
+// in stream order for this call.
 template <bool ANY>
 int launch_trace(const ckr_scene *s, const ckr_ray *rays, uint32_t n, uint32_t *hit_id, float *hit_t,
-                 uint8_t *occluded, cudaStream_t stream) {
+                 uint8_t *occluded, cudaStream_t stream, uint32_t *next = nullptr) {
   if (n == 0) return CKR_OK;
-  LaunchShape ls;
-  CKR_CUDA_TRY(launch_shape<ANY>(s, n, ls));
-  // The ray counter is stream-ordered scratch, so concurrent calls on other streams
-  // cannot share it.
+  const int grid = s->trace_grid[ANY ? 1 : 0];
+  const size_t smem = s->trace_smem;
+  // The attribute is per kernel: set it for this scene's stack before each launch.
+  if (smem > 48 * 1024)
+    CKR_CUDA_TRY(cudaFuncSetAttribute(k_trace_dyn<ANY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   // Launches cover at most 2^31 rays so that the counter, which overshoots n by at
   // most one refill per warp, cannot wrap.
-  uint32_t *next = nullptr;
-  CKR_CUDA_TRY(cudaMallocAsync((void **)&next, sizeof(uint32_t), stream));
+  const bool own = next == nullptr;
+  if (own) CKR_CUDA_TRY(cudaMallocAsync((void **)&next, sizeof(uint32_t), stream));
   cudaError_t e = cudaSuccess;
   constexpr uint32_t kChunk = 1u << 31;
   for (uint32_t off = 0; off < n && e == cudaSuccess; off += std::min(n - off, kChunk)) {
     const uint32_t m = std::min(n - off, kChunk);
     e = cudaMemsetAsync(next, 0, sizeof(uint32_t), stream);
     if (e != cudaSuccess) break;
-    k_trace_dyn<ANY><<<ls.grid, kTPB, ls.smem, stream>>>(
+    k_trace_dyn<ANY><<<grid, kTPB, smem, stream>>>(
         view_of(s), reinterpret_cast<const float4 *>(rays + off), m, ANY ? nullptr : hit_id + off,
         ANY ? nullptr : hit_t + off, ANY ? occluded + off : nullptr, (int)stack_depth_of(s), next);
     e = cudaGetLastError();
     if (n - off <= kChunk) break;
   }
-  cudaFreeAsync(next, stream);
+  if (own) cudaFreeAsync(next, stream);
   CKR_CUDA_TRY(e);
   return CKR_OK;
 }
@@ -198,6 +203,11 @@ extern "C" int ckr_scene_create(const float *tri9, uint32_t ntri, const float *s
       return fail(CKR_ERR_CUDA);
   }
   if (cudaMemset(s->status.ptr, 0, sizeof(int)) != cudaSuccess) return fail(CKR_ERR_CUDA);
+  LaunchShape l0, l1;
+  if (launch_shape<false>(s, l0) != cudaSuccess || launch_shape<true>(s, l1) != cudaSuccess) return fail(CKR_ERR_CUDA);
+  s->trace_grid[0] = l0.grid;
+  s->trace_grid[1] = l1.grid;
+  s->trace_smem = l0.smem;
   s->host_nodes.swap(bvh.nodes);
   s->host_tris.swap(bvh.tris);
   *out = s;
@@ -208,8 +218,9 @@ extern "C" int ckr_scene_destroy(ckr_scene *scene) {
   if (!scene) return CKR_ERR_INVALID_ARGUMENT;
   for (auto &st : scene->pipe)
     if (st) cudaStreamDestroy(st);
-  for (auto &e : scene->ev)
+  for (auto &e : scene->pipe_done)
     if (e) cudaEventDestroy(e);
+  if (scene->user_ready) cudaEventDestroy(scene->user_ready);
   if (scene->render_ws && scene->render_ws_free) scene->render_ws_free(scene->render_ws);
   delete scene;
   return CKR_OK;
@@ -252,41 +263,51 @@ extern "C" int ckr_trace_any(const ckr_scene *s, const ckr_ray *rays, uint32_t n
 
 namespace {
 
-// Host-buffer path: two internal streams alternate over chunks so that the
-// copy of chunk k+1 overlaps the traversal of chunk k.
+// Host-buffer path: kPipes internal streams take turns over chunks of kHostChunk
+// rays, so that the host-to-device copy of one chunk and the device-to-host copy
+// of another overlap the traversal of a third; each stream has its own staging
+// slot and ray counter.  Swept on the 2^23-ray workload (e2e Mrays/s): 2 x 2^19
+// 2530, 2 x 2^20 2899, 2 x 2^21 2983, 3 x 2^19 2999, 3 x 2^20 3089, 3 x 2^21 2987,
+// 4 x 2^20 3086.
+constexpr int kPipes = 3;
+constexpr uint32_t kHostChunk = 1u << 20;
+
 template <bool ANY>
 int trace_host(ckr_scene *s, const ckr_ray *rays, uint32_t n, uint32_t *hit_id, float *hit_t, uint8_t *occ,
                cudaStream_t user) {
+  static_assert(kPipes <= ckr_scene::kMaxPipes, "pipeline streams");
   if (n == 0) return CKR_OK;
   std::lock_guard<std::mutex> lock(s->host_mu);
-  const uint32_t chunk = 1u << 20;
-  uint32_t cap = std::min(n, 2 * chunk);
+  const uint32_t chunk = kHostChunk;
+  uint32_t cap = (uint32_t)std::min<uint64_t>(n, (uint64_t)kPipes * chunk);
   CKR_CUDA_TRY(s->st_rays.reserve(cap));
+  CKR_CUDA_TRY(s->st_next.reserve(kPipes));
   if (ANY) {
     CKR_CUDA_TRY(s->st_occ.reserve(cap));
   } else {
     CKR_CUDA_TRY(s->st_id.reserve(cap));
     CKR_CUDA_TRY(s->st_t.reserve(cap));
   }
-  for (int k = 0; k < 2; ++k)
+  for (int k = 0; k < kPipes; ++k) {
     if (!s->pipe[k]) CKR_CUDA_TRY(cudaStreamCreateWithFlags(&s->pipe[k], cudaStreamNonBlocking));
-  for (int k = 0; k < 4; ++k)
-    if (!s->ev[k]) CKR_CUDA_TRY(cudaEventCreateWithFlags(&s->ev[k], cudaEventDisableTiming));
+    if (!s->pipe_done[k]) CKR_CUDA_TRY(cudaEventCreateWithFlags(&s->pipe_done[k], cudaEventDisableTiming));
+  }
+  if (!s->user_ready) CKR_CUDA_TRY(cudaEventCreateWithFlags(&s->user_ready, cudaEventDisableTiming));
   // Order after prior work on the caller's stream.
-  CKR_CUDA_TRY(cudaEventRecord(s->ev[2], user));
-  CKR_CUDA_TRY(cudaStreamWaitEvent(s->pipe[0], s->ev[2], 0));
-  CKR_CUDA_TRY(cudaStreamWaitEvent(s->pipe[1], s->ev[2], 0));
+  CKR_CUDA_TRY(cudaEventRecord(s->user_ready, user));
+  for (int k = 0; k < kPipes; ++k) CKR_CUDA_TRY(cudaStreamWaitEvent(s->pipe[k], s->user_ready, 0));
   uint32_t k = 0;
   for (uint32_t off = 0; off < n; off += chunk, ++k) {
     uint32_t m = std::min(chunk, n - off);
-    int slot = k & 1;
+    int slot = (int)(k % kPipes);
     cudaStream_t st = s->pipe[slot];
     size_t base = (size_t)slot * chunk;
     CKR_CUDA_TRY(cudaMemcpyAsync(s->st_rays.ptr + base, rays + off, (size_t)m * sizeof(ckr_ray),
                                  cudaMemcpyHostToDevice, st));
-    int rc = ANY ? launch_trace<true>(s, s->st_rays.ptr + base, m, nullptr, nullptr, s->st_occ.ptr + base, st)
+    int rc = ANY ? launch_trace<true>(s, s->st_rays.ptr + base, m, nullptr, nullptr, s->st_occ.ptr + base, st,
+                                      s->st_next.ptr + slot)
                  : launch_trace<false>(s, s->st_rays.ptr + base, m, s->st_id.ptr + base, s->st_t.ptr + base,
-                                       nullptr, st);
+                                       nullptr, st, s->st_next.ptr + slot);
     if (rc != CKR_OK) return rc;
     if (ANY) {
       CKR_CUDA_TRY(cudaMemcpyAsync(occ + off, s->st_occ.ptr + base, m, cudaMemcpyDeviceToHost, st));
@@ -294,11 +315,12 @@ int trace_host(ckr_scene *s, const ckr_ray *rays, uint32_t n, uint32_t *hit_id, 
       CKR_CUDA_TRY(cudaMemcpyAsync(hit_id + off, s->st_id.ptr + base, (size_t)m * 4, cudaMemcpyDeviceToHost, st));
       CKR_CUDA_TRY(cudaMemcpyAsync(hit_t + off, s->st_t.ptr + base, (size_t)m * 4, cudaMemcpyDeviceToHost, st));
     }
+    if (n - off <= chunk) break;
   }
-  CKR_CUDA_TRY(cudaEventRecord(s->ev[0], s->pipe[0]));
-  CKR_CUDA_TRY(cudaEventRecord(s->ev[1], s->pipe[1]));
-  CKR_CUDA_TRY(cudaStreamWaitEvent(user, s->ev[0], 0));
-  CKR_CUDA_TRY(cudaStreamWaitEvent(user, s->ev[1], 0));
+  for (int k = 0; k < kPipes; ++k) {
+    CKR_CUDA_TRY(cudaEventRecord(s->pipe_done[k], s->pipe[k]));
+    CKR_CUDA_TRY(cudaStreamWaitEvent(user, s->pipe_done[k], 0));
+  }
   CKR_CUDA_TRY(cudaStreamSynchronize(user));
   int h = 0;
   CKR_CUDA_TRY(cudaMemcpy(&h, s->status.ptr, sizeof(int), cudaMemcpyDeviceToHost));

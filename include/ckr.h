@@ -61,7 +61,8 @@ typedef struct ckr_ray {
 typedef struct ckr_scene ckr_scene;
 
 typedef struct ckr_build_params {
-  uint32_t max_leaf_size; /* triangles per leaf, 1..8; 0 = default (4) */
+  uint32_t max_leaf_size; /* triangles per leaf of the wide tree, 1..8 accepted, capped at 3;
+                             0 = default (3) */
   uint32_t sah_bins;      /* binned-SAH bins, 4..64; 0 = default (16) */
   uint32_t threads;       /* host build threads; 0 = all cores */
 } ckr_build_params;

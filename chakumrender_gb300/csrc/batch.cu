@@ -30,7 +30,7 @@ struct BatchWs {
     size_t sh = w * per_path;
     if (ray_o.reserve(w) || ray_d.reserve(w) || beta.reserve(w) || meta.reserve(w) || hit_id.reserve(w) ||
         hit_t.reserve(w) || q0.reserve(w) || q1.reserve(w) || sh_o.reserve(sh) || sh_d.reserve(sh) ||
-        sh_c.reserve(sh) || sh_px.reserve(sh) || counts.reserve(4) || stats.reserve(2))
+        sh_c.reserve(sh) || sh_px.reserve(sh) || counts.reserve(8) || stats.reserve(2))
       return CKR_ERR_OUT_OF_MEMORY;
     wave = w;
     shadow = sh;
@@ -136,12 +136,17 @@ int enqueue(ckr_batch *b, JobSet &set, bool pack, size_t wave, cudaStream_t stre
   ckr_scene *s = b->scene;
   const int depth = (int)stack_depth_of(s);
   const size_t smem = (size_t)depth * TPB * sizeof(uint2);
+  // Deep trees: dynamic fetching; one or two levels: one ray per thread.
+  const bool dyn = s->max_depth >= kDynamicDepth;
+  void (*const extend_fn)(SceneView, Paths, int, int) = dyn ? k_extend<TPB, true> : k_extend<TPB, false>;
+  void (*const shadow_fn)(SceneView, Paths, int, int, float4 *) =
+      dyn ? k_shadow<TPB, true> : k_shadow<TPB, false>;
   if (smem > 48 * 1024) {
-    CKR_CUDA_TRY(cudaFuncSetAttribute(k_extend<TPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CKR_CUDA_TRY(cudaFuncSetAttribute(k_shadow<TPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CKR_CUDA_TRY(cudaFuncSetAttribute(extend_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CKR_CUDA_TRY(cudaFuncSetAttribute(shadow_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
-  const int g_ext = grid_for((const void *)k_extend<TPB>, smem, TPB);
-  const int g_sh = grid_for((const void *)k_shadow<TPB>, smem, TPB);
+  const int g_ext = grid_for((const void *)extend_fn, smem, TPB);
+  const int g_sh = grid_for((const void *)shadow_fn, smem, TPB);
   const bool nee = b->shader == CKR_SHADER_PATH_NEE;
   const int g_shade = grid_for(nee ? (const void *)k_shade_nee<TPB> : (const void *)k_shade<CKR_SHADER_PATH, TPB>,
                                0, TPB);
@@ -176,12 +181,14 @@ int enqueue(ckr_batch *b, JobSet &set, bool pack, size_t wave, cudaStream_t stre
       ++n_launch;
       int cur = 0;
       for (uint32_t d = 0; d <= dmax; ++d) {
-        k_extend<TPB><<<g_ext, TPB, smem, stream>>>(sv, P, cur, depth);
+        // Work counters of k_extend and k_shadow (P.counts[3], [4]).
+        CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 3, 0, 2 * sizeof(uint32_t), stream));
+        extend_fn<<<g_ext, TPB, smem, stream>>>(sv, P, cur, depth);
         CKR_CUDA_TRY(cudaMemsetAsync(P.counts + (cur ^ 1), 0, sizeof(uint32_t), stream));
         CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), stream));
         if (nee) k_shade_nee<TPB><<<g_shade, TPB, 0, stream>>>(shv, P, prm, cur, Learn{});
         else k_shade<CKR_SHADER_PATH, TPB><<<g_shade, TPB, 0, stream>>>(shv, P, prm, cur, (int)d, nullptr);
-        k_shadow<TPB><<<g_sh, TPB, smem, stream>>>(sv, P, depth, cur, nullptr);
+        shadow_fn<<<g_sh, TPB, smem, stream>>>(sv, P, depth, cur, nullptr);
         n_launch += 3;
         cur ^= 1;
       }

@@ -117,7 +117,7 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   CKR_CUDA_TRY(W.sh_d.reserve(shadow));
   CKR_CUDA_TRY(W.sh_c.reserve(shadow));
   CKR_CUDA_TRY(W.sh_px.reserve(shadow));
-  CKR_CUDA_TRY(W.counts.reserve(4));
+  CKR_CUDA_TRY(W.counts.reserve(8));
   if (!W.stats.ptr) {
     CKR_CUDA_TRY(W.stats.reserve(2));
     CKR_CUDA_TRY(cudaMemset(W.stats.ptr, 0, 2 * sizeof(unsigned long long)));
@@ -157,12 +157,17 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   ShadeView shv = shade_view_of(s);
   int depth = (int)stack_depth_of(s);
   size_t smem = (size_t)depth * kRTPB * sizeof(uint2);
+  // Deep trees: dynamic fetching; one or two levels: one ray per thread.
+  const bool dyn = s->max_depth >= kDynamicDepth;
+  void (*const extend_fn)(SceneView, Paths, int, int) = dyn ? k_extend<kRTPB, true> : k_extend<kRTPB, false>;
+  void (*const shadow_fn)(SceneView, Paths, int, int, float4 *) =
+      dyn ? k_shadow<kRTPB, true> : k_shadow<kRTPB, false>;
   if (smem > 48 * 1024) {
-    CKR_CUDA_TRY(cudaFuncSetAttribute(k_extend<kRTPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CKR_CUDA_TRY(cudaFuncSetAttribute(k_shadow<kRTPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CKR_CUDA_TRY(cudaFuncSetAttribute(extend_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CKR_CUDA_TRY(cudaFuncSetAttribute(shadow_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
-  const int g_ext = grid_for((const void *)k_extend<kRTPB>, smem, kRTPB);
-  const int g_sh = grid_for((const void *)k_shadow<kRTPB>, smem, kRTPB);
+  const int g_ext = grid_for((const void *)extend_fn, smem, kRTPB);
+  const int g_sh = grid_for((const void *)shadow_fn, smem, kRTPB);
   if (cfg->shader == CKR_SHADER_EXPLICIT && smem > 48 * 1024)
     CKR_CUDA_TRY(cudaFuncSetAttribute(k_shade<CKR_SHADER_EXPLICIT, kRTPB>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -178,7 +183,9 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
     k_camera<kRTPB><<<std::min<int>(g_ext, ceil_div(n, kRTPB)), kRTPB, 0, stream>>>(c, P, prm, base, n);
     int cur = 0;
     for (uint32_t d = 0; d <= prm.max_depth; ++d) {
-      k_extend<kRTPB><<<g_ext, kRTPB, smem, stream>>>(sv, P, cur, depth);
+      // Work counters of k_extend and k_shadow (P.counts[3], [4]).
+      CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 3, 0, 2 * sizeof(uint32_t), stream));
+      extend_fn<<<g_ext, kRTPB, smem, stream>>>(sv, P, cur, depth);
       CKR_CUDA_TRY(cudaMemsetAsync(P.counts + (cur ^ 1), 0, sizeof(uint32_t), stream));
       CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), stream));
       Learn lr{};
@@ -215,7 +222,7 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
         k_shade<CKR_SHADER_DIRECT_MIS, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else
         k_shade<CKR_SHADER_DIRECT_MISCV, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
-      k_shadow<kRTPB><<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur, train ? prop->rec.ptr : nullptr);
+      shadow_fn<<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur, train ? prop->rec.ptr : nullptr);
       if (train) {
         // Adam steps on this bounce's light samples (visibility applied above),
         // minibatch by minibatch; steps past the records actually written are no-ops.
@@ -392,11 +399,11 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
   P.sh_d = reinterpret_cast<float4 *>(take(16ull * kNoAllocShadow));
   P.sh_c = reinterpret_cast<float4 *>(take(16ull * kNoAllocShadow));
   P.sh_px = reinterpret_cast<uint32_t *>(take(4ull * kNoAllocShadow));
-  P.counts = reinterpret_cast<uint32_t *>(take(16));
+  P.counts = reinterpret_cast<uint32_t *>(take(32));
   P.stats = reinterpret_cast<unsigned long long *>(take(16));
   P.accum = reinterpret_cast<double *>(take(24ull * kNoAllocMaxPixels));
   // The arena keeps the previous call's contents: clear what must start at zero.
-  CKR_CUDA_TRY(cudaMemsetAsync(P.counts, 0, 16, stream));
+  CKR_CUDA_TRY(cudaMemsetAsync(P.counts, 0, 32, stream));
   CKR_CUDA_TRY(cudaMemsetAsync(P.stats, 0, 16, stream));
   CKR_CUDA_TRY(cudaMemsetAsync(P.accum, 0, sizeof(double) * 3 * (size_t)prm.npix, stream));
   Cam c;
@@ -411,12 +418,17 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
   const LtcEntry *ltc = g_noalloc_ltc_dev[dev];
   int depth = (int)stack_depth_of(s);
   size_t smem = (size_t)depth * kRTPB * sizeof(uint2);
+  // Deep trees: dynamic fetching; one or two levels: one ray per thread.
+  const bool dyn = s->max_depth >= kDynamicDepth;
+  void (*const extend_fn)(SceneView, Paths, int, int) = dyn ? k_extend<kRTPB, true> : k_extend<kRTPB, false>;
+  void (*const shadow_fn)(SceneView, Paths, int, int, float4 *) =
+      dyn ? k_shadow<kRTPB, true> : k_shadow<kRTPB, false>;
   if (smem > 48 * 1024) {
-    CKR_CUDA_TRY(cudaFuncSetAttribute(k_extend<kRTPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CKR_CUDA_TRY(cudaFuncSetAttribute(k_shadow<kRTPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CKR_CUDA_TRY(cudaFuncSetAttribute(extend_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CKR_CUDA_TRY(cudaFuncSetAttribute(shadow_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
-  const int g_ext = grid_for((const void *)k_extend<kRTPB>, smem, kRTPB);
-  const int g_sh = grid_for((const void *)k_shadow<kRTPB>, smem, kRTPB);
+  const int g_ext = grid_for((const void *)extend_fn, smem, kRTPB);
+  const int g_sh = grid_for((const void *)shadow_fn, smem, kRTPB);
   const void *shade_fn = cfg->shader == CKR_SHADER_PATH_NEE ? (const void *)k_shade_nee<kRTPB>
                          : cfg->shader == CKR_SHADER_PATH      ? (const void *)k_shade<CKR_SHADER_PATH, kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_CV  ? (const void *)k_shade<CKR_SHADER_DIRECT_CV, kRTPB>
@@ -428,7 +440,9 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
     k_camera<kRTPB><<<std::min<int>(g_ext, ceil_div(n, kRTPB)), kRTPB, 0, stream>>>(c, P, prm, base, n);
     int cur = 0;
     for (uint32_t d = 0; d <= prm.max_depth; ++d) {
-      k_extend<kRTPB><<<g_ext, kRTPB, smem, stream>>>(sv, P, cur, depth);
+      // Work counters of k_extend and k_shadow (P.counts[3], [4]).
+      CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 3, 0, 2 * sizeof(uint32_t), stream));
+      extend_fn<<<g_ext, kRTPB, smem, stream>>>(sv, P, cur, depth);
       CKR_CUDA_TRY(cudaMemsetAsync(P.counts + (cur ^ 1), 0, sizeof(uint32_t), stream));
       CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), stream));
       if (cfg->shader == CKR_SHADER_PATH_NEE)
@@ -441,7 +455,7 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
         k_shade<CKR_SHADER_DIRECT_MIS, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else
         k_shade<CKR_SHADER_DIRECT_MISCV, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
-      k_shadow<kRTPB><<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur, nullptr);
+      shadow_fn<<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur, nullptr);
       cur ^= 1;
       if (!path) break;
     }

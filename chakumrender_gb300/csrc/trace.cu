@@ -35,63 +35,28 @@ namespace {
 
 constexpr int kTPB = 128;
 
-// Closest / any hit with dynamic ray fetching (after Aila and Laine, "Understanding
-// the Efficiency of Ray Traversal on GPUs", HPG 2009): a lane whose ray is finished
-// takes the next ray from a global counter (one atomic per warp refill) instead of
-// idling until its whole warp is done; each loop iteration advances every active lane
-// by one wide node and/or one triangle (trace_step).
-constexpr int kRefill = 8;  // refill once this many lanes of a warp are idle
-
+// Closest / any hit over a ray array, with dynamic ray fetching (trace_dynamic).
 template <bool ANY>
 __global__ void __launch_bounds__(kTPB) k_trace_dyn(SceneView s, const float4 *__restrict__ rays, uint32_t n,
                                                     uint32_t *__restrict__ hit_id, float *__restrict__ hit_t,
                                                     uint8_t *__restrict__ occluded, int depth, uint32_t *next) {
   extern __shared__ uint2 smem_trav[];
-  uint2 *stack = smem_trav + threadIdx.x;
-  const uint32_t lane = threadIdx.x & 31u;
-  RayPre r{};
-  float tbest = 0.f;
-  uint32_t best = kMiss, idx = 0;
-  Trav st{};
-  bool active = false, live = false, more = true;
-  for (;;) {
-    const unsigned idle = __ballot_sync(0xffffffffu, !active);
-    if (more && (idle == 0xffffffffu || __popc(idle) >= kRefill)) {
-      const uint32_t want = (uint32_t)__popc(idle);
-      uint32_t base = 0;
-      if (lane == 0) base = atomicAdd(next, want);
-      base = __shfl_sync(0xffffffffu, base, 0);
-      if ((uint64_t)base + want >= n) more = false;
-      if (!active) {
-        idx = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
-        if (idx < n) {
-          float4 a = __ldg(rays + 2 * (size_t)idx), b = __ldg(rays + 2 * (size_t)idx + 1);
-          r = make_ray(a, b);
-          tbest = b.w;
-          best = kMiss;
-          st = trav_start(s, r);
-          live = trace_spheres<ANY>(s, r, tbest, best);
-          active = true;
-        }
-      }
-    }
-    if (!__any_sync(0xffffffffu, active)) {
-      if (!more) break;
-      continue;  // every lane idle: the next iteration refills the whole warp
-    }
-    if (active) {
-      if (live) live = trace_step<ANY>(s, r, tbest, best, st, stack, kTPB, depth);
-      if (!live) {
+  trace_dynamic<ANY>(
+      s, n, next, smem_trav + threadIdx.x, kTPB, depth,
+      [&](uint32_t i, RayPre &r, float &tmax) {
+        const float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
+        r = make_ray(a, b);
+        tmax = b.w;
+        return true;
+      },
+      [&](uint32_t i, uint32_t best, float t) {
         if (ANY) {
-          occluded[idx] = best != kMiss ? 1 : 0;
+          occluded[i] = best != kMiss ? 1 : 0;
         } else {
-          hit_id[idx] = best;
-          hit_t[idx] = tbest;
+          hit_id[i] = best;
+          hit_t[i] = t;
         }
-        active = false;
-      }
-    }
-  }
+      });
 }
 
 struct LaunchShape {

@@ -65,7 +65,8 @@ struct Paths {
   uint32_t *sh_px;
   uint32_t *prev_row;  // learned selection: the path's row in the previous bounce's probabilities
   uint32_t *sh_rec;    // training: per shadow ray, its training record (kNoRec: none)
-  uint32_t *counts;  // [0] q[0] length, [1] q[1] length, [2] shadow count
+  uint32_t *counts;  // [0] q[0] length, [1] q[1] length, [2] shadow count, [3] [4] work counters of
+                     // k_extend and k_shadow (zeroed before each k_extend)
   unsigned long long *stats;  // cumulative closest-hit rays, shadow rays
   double *accum;     // 3 per output pixel
 };
@@ -178,46 +179,68 @@ __global__ void __launch_bounds__(TPB) k_camera(Cam cam0, Paths P, Params prm, u
   if (blockIdx.x == 0 && threadIdx.x == 0) P.counts[0] = wave_n;
 }
 
-template <int TPB>
+// Trees at least this many levels deep are traversed with dynamic fetching
+// (trace_dynamic); shallower ones with one ray per thread (trace_static).  Box
+// scene (one level), 256^2 x 16 spp: 1.64 ms static, 1.75 ms dynamic; many-light
+// scene (eight levels), 960x540 x 16 spp: 26.3 ms static, 23.0 ms dynamic.
+constexpr uint32_t kDynamicDepth = 3;
+
+// Closest hit of the paths in queue `cur`.  DYN: dynamic fetching over the queue,
+// work counter P.counts[3] (zeroed before the launch).
+template <int TPB, bool DYN>
 __global__ void __launch_bounds__(TPB) k_extend(SceneView s, Paths P, int cur, int depth) {
   extern __shared__ uint2 smem_trav[];
-  uint2 *stack = smem_trav + threadIdx.x;
-  const uint32_t n = P.counts[cur];
   const uint32_t *q = cur ? P.q1 : P.q0;
-  for (uint32_t i = blockIdx.x * TPB + threadIdx.x; i < n; i += gridDim.x * TPB) {
-    uint32_t slot = q[i];
-    float4 a = P.ray_o[slot], b = P.ray_d[slot];
-    if (a.w < 0.f) continue;  // traced by the shading kernel (CKR_SHADER_EXPLICIT)
-    RayPre r = make_ray(a, b);
-    float t = b.w;
-    uint32_t id = trace_ray<false>(s, r, t, stack, TPB, depth);
-    P.hit_id[slot] = id;
+  auto fetch = [&](uint32_t i, RayPre &r, float &tmax) {
+    const uint32_t slot = q[i];
+    const float4 a = P.ray_o[slot], b = P.ray_d[slot];
+    if (a.w < 0.f) return false;  // traced by the shading kernel (CKR_SHADER_EXPLICIT)
+    r = make_ray(a, b);
+    tmax = b.w;
+    return true;
+  };
+  auto finish = [&](uint32_t i, uint32_t best, float t) {
+    const uint32_t slot = q[i];
+    P.hit_id[slot] = best;
     P.hit_t[slot] = t;
-  }
+  };
+  if (DYN)
+    trace_dynamic<false>(s, P.counts[cur], P.counts + 3, smem_trav + threadIdx.x, TPB, depth, fetch, finish);
+  else
+    trace_static<false, TPB>(s, P.counts[cur], smem_trav + threadIdx.x, depth, fetch, finish);
 }
 
-template <int TPB>
+// Any hit of the shadow queue: unoccluded rays add their contribution to the
+// pixel; occluded ones zero their training record's weight.  DYN: dynamic
+// fetching, work counter P.counts[4] (zeroed before the launch).
+template <int TPB, bool DYN>
 __global__ void __launch_bounds__(TPB) k_shadow(SceneView s, Paths P, int depth, int cur, float4 *rec) {
   extern __shared__ uint2 smem_trav[];
-  uint2 *stack = smem_trav + threadIdx.x;
   const uint32_t n = P.counts[2];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     // Ray statistics: closest-hit rays of this bounce and its shadow rays.
     atomicAdd(&P.stats[0], (unsigned long long)P.counts[cur]);
     atomicAdd(&P.stats[1], (unsigned long long)n);
   }
-  for (uint32_t i = blockIdx.x * TPB + threadIdx.x; i < n; i += gridDim.x * TPB) {
-    float4 a = P.sh_o[i], b = P.sh_d[i];
-    RayPre r = make_ray(a, b);
-    float t = b.w;
-    if (trace_ray<true>(s, r, t, stack, TPB, depth) == kMiss) {
-      float4 c = P.sh_c[i];
+  auto fetch = [&](uint32_t i, RayPre &r, float &tmax) {
+    const float4 a = P.sh_o[i], b = P.sh_d[i];
+    r = make_ray(a, b);
+    tmax = b.w;
+    return true;
+  };
+  auto finish = [&](uint32_t i, uint32_t best, float) {
+    if (best == kMiss) {
+      const float4 c = P.sh_c[i];
       add_px(P.accum, P.sh_px[i], f3(c.x, c.y, c.z));
     } else if (rec) {
-      uint32_t ri = P.sh_rec[i];
+      const uint32_t ri = P.sh_rec[i];
       if (ri != kNoRec) rec[3 * (size_t)ri + 1].w = 0.f;  // occluded: the sample contributed nothing
     }
-  }
+  };
+  if (DYN)
+    trace_dynamic<true>(s, n, P.counts + 4, smem_trav + threadIdx.x, TPB, depth, fetch, finish);
+  else
+    trace_static<true, TPB>(s, n, smem_trav + threadIdx.x, depth, fetch, finish);
 }
 
 // Light-technique samples at one surface: returns the number of shadow rays

@@ -20,6 +20,9 @@ CKR_MISS = 0xFFFFFFFF
 CKR_SPHERE_BIT = 0x80000000
 
 
+CKR_ERR_INVALID_ARGUMENT, CKR_ERR_PARSE, CKR_ERR_IO, CKR_ERR_TOO_LARGE = -1, -8, -9, -10
+
+
 class CkrError(RuntimeError):
     def __init__(self, status: int, what: str):
         self.status = status
@@ -67,6 +70,10 @@ def lib() -> C.CDLL:
     _sig(L, "ckr_trace_closest_host", [P, P, U32, P, P, P])
     _sig(L, "ckr_trace_any_host", [P, P, U32, P, P])
     _sig(L, "ckr_trace_stats", [P, P, U32, C.POINTER(C.c_double), C.POINTER(C.c_double)])
+    _sig(L, "ckr_obj_load", [C.c_char_p, P, U32, C.POINTER(U32)])
+    _sig(L, "ckr_read_ppm_p6", [C.c_char_p, P, U32, C.POINTER(U32), C.POINTER(U32)])
+    _sig(L, "ckr_write_ppm_p6", [C.c_char_p, P, U32, U32])
+    _sig(L, "ckr_write_pfm", [C.c_char_p, P, U32, U32])
     _sig(L, "ckr_workload_icosphere", [U32, F32, U32, C.c_uint64, P, U32, C.POINTER(U32)])
     _sig(L, "ckr_workload_rays_pinhole", [P, P, P, F32, U32, U32, F32, P])
     _sig(L, "ckr_workload_rays_incoherent", [P, P, C.c_uint64, U32, F32, F32, P])
@@ -129,6 +136,39 @@ def _f3(v) -> np.ndarray:
 
 
 # ---- synthetic workloads ---------------------------------------------------------
+def load_obj(path) -> np.ndarray:
+    """Triangles of a Wavefront OBJ file as an (n, 9) float32 array (ckr_obj_load)."""
+    L = lib()
+    n = U32(0)
+    p = str(path).encode()
+    check(L.ckr_obj_load(p, None, 0, C.byref(n)), "ckr_obj_load size")
+    out = np.empty((n.value, 9), dtype=np.float32)
+    if n.value:
+        check(L.ckr_obj_load(p, _ptr(out), n.value, C.byref(n)), "ckr_obj_load")
+    return out
+
+
+def read_ppm_p6(path) -> np.ndarray:
+    """(h, w, 3) float32 image of a binary P6 file (ckr_read_ppm_p6)."""
+    L = lib()
+    w, h = U32(0), U32(0)
+    p = str(path).encode()
+    check(L.ckr_read_ppm_p6(p, None, 0, C.byref(w), C.byref(h)), "ckr_read_ppm_p6 size")
+    out = np.empty((h.value, w.value, 3), dtype=np.float32)
+    check(L.ckr_read_ppm_p6(p, _ptr(out), w.value * h.value, C.byref(w), C.byref(h)), "ckr_read_ppm_p6")
+    return out
+
+
+def write_ppm_p6(path, rgb: np.ndarray) -> None:
+    rgb = np.ascontiguousarray(rgb, dtype=np.float32)
+    check(lib().ckr_write_ppm_p6(str(path).encode(), _ptr(rgb), rgb.shape[1], rgb.shape[0]), "ckr_write_ppm_p6")
+
+
+def write_pfm(path, rgb: np.ndarray) -> None:
+    rgb = np.ascontiguousarray(rgb, dtype=np.float32)
+    check(lib().ckr_write_pfm(str(path).encode(), _ptr(rgb), rgb.shape[1], rgb.shape[0]), "ckr_write_pfm")
+
+
 def icosphere(subdiv: int = 8, noise_amp: float = 0.05, octaves: int = 6, seed: int = 1) -> np.ndarray:
     L = lib()
     n = U32(0)

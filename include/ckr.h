@@ -364,6 +364,29 @@ int ckr_xml_free(ckr_xml_scene *scene);
 /* P3 PPM of src/main.cpp:98-117: clamp to [0, 1], gamma 1/2.2, int(x*255+.5). */
 int ckr_write_ppm(const char *path, const float *rgb, uint32_t width, uint32_t height);
 
+/* Binary P6 PPM, replacing readImage / writeImage (headers/ppm.h:6-7,
+ * src/ppm.cpp:36-152; the reference reads and writes the fixed names env1.ppm
+ * and env1_cpy.ppm).  Read: "P6", comment lines, width, height, maxval 255 (else
+ * CKR_ERR_PARSE), then bytes b -> b / 255 into rgb (w * h * 3 floats, row 0 first);
+ * rgb = NULL returns the size only, capacity_px < w * h gives CKR_ERR_TOO_LARGE.
+ * Write: clamp to [0, 1] and truncate x * 255 (no gamma, as writeImage). */
+int ckr_read_ppm_p6(const char *path, float *rgb, uint32_t capacity_px, uint32_t *width, uint32_t *height);
+int ckr_write_ppm_p6(const char *path, const float *rgb, uint32_t width, uint32_t height);
+
+/* HDR output (no reference counterpart; the reference writes only 8-bit P3):
+ * linear FP32 PFM ("PF", little- or big-endian by the host, rows bottom to top)
+ * of the same rgb layout as ckr_write_ppm (row 0 = top of the image). */
+int ckr_write_pfm(const char *path, const float *rgb, uint32_t width, uint32_t height);
+
+/* Wavefront OBJ geometry, written from the public format (the reference carries
+ * an unused loader, externLib/objectLoader, and no OBJ asset): `v` vertices and
+ * `f` polygons (corners v, v/vt, v//vn, v/vt/vn; 1-based or negative indices),
+ * triangulated as fans; other statements skipped.  tri9 = NULL returns the
+ * triangle count in *ntri; else up to `capacity` triangles (A.xyz B.xyz C.xyz)
+ * are written and CKR_ERR_TOO_LARGE reports a short buffer.  CKR_ERR_IO: the file
+ * cannot be read; CKR_ERR_PARSE: a malformed v or f line or an index out of range. */
+int ckr_obj_load(const char *path, float *tri9, uint32_t capacity, uint32_t *ntri);
+
 /* ---- LTC polygon-light shading ------------------------------------------ */
 /* Loads the GGX LTC fit table (the reference's headers/ltc.inc, converted to
  * data/ltc_ggx.bin).  NULL: the copy beside libckr.so.  Optional: the first

@@ -73,6 +73,8 @@ def ref() -> C.CDLL:
         _sig(L, "ref_trace_build", [P, U32])
         _sig(L, "ref_trace_closest", [P, U32, P, P, C.c_int], None)
         _sig(L, "ref_trace_shadow", [P, U32, P, C.c_int], None)
+        _sig(L, "ref_read_image", [C.c_char_p, P, U32, P, P])
+        _sig(L, "ref_write_image", [C.c_char_p, P, U32, U32])
         _ref = L
     return _ref
 

@@ -219,3 +219,43 @@ void ref_ltc_shade_batch(const RefMaterialRow *m, uint32_t count, const double *
 }
 
 }  // extern "C"
+
+// ---- P6 images: readImage / writeImage (src/ppm.cpp:36-152) ----------------
+// The reference reads ./env1.ppm and writes ./env1_cpy.ppm; these run it with the
+// working directory set to `dir` for the call.
+#include <unistd.h>
+#include "ppm.h"
+
+extern "C" {
+
+int ref_read_image(const char *dir, double *rgb, uint32_t cap_px, uint32_t *w, uint32_t *h) {
+  char old[4096];
+  if (!getcwd(old, sizeof(old)) || chdir(dir) != 0) return -1;
+  Vec *image = 0;
+  uint32_t ww = 0, hh = 0;
+  int ok = readImage(image, ww, hh);
+  if (chdir(old) != 0) return -1;
+  if (!ok) return -2;
+  *w = ww;
+  *h = hh;
+  if ((uint64_t)ww * hh > cap_px) return -3;
+  for (uint64_t i = 0; i < (uint64_t)ww * hh; ++i) {
+    rgb[3 * i] = image[i].x;
+    rgb[3 * i + 1] = image[i].y;
+    rgb[3 * i + 2] = image[i].z;
+  }
+  delete[] image;
+  return 0;
+}
+
+int ref_write_image(const char *dir, const double *rgb, uint32_t w, uint32_t h) {
+  char old[4096];
+  if (!getcwd(old, sizeof(old)) || chdir(dir) != 0) return -1;
+  std::vector<Vec> image((size_t)w * h);
+  for (size_t i = 0; i < image.size(); ++i) image[i] = Vec(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
+  int ok = writeImage(image.data(), w, h);
+  if (chdir(old) != 0) return -1;
+  return ok ? 0 : -2;
+}
+
+}  // extern "C"

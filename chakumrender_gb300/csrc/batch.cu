@@ -288,7 +288,7 @@ extern "C" int ckr_batch_create(ckr_scene *s, uint32_t shader, float rr_prob, ui
   b->shader = shader;
   b->rr_prob = rr_prob;
   b->n_light = std::max(1u, n_light_samples);
-  b->per_path = shader == CKR_SHADER_PATH_NEE ? 1u : std::max(1u, points + area * b->n_light);
+  b->per_path = shader == CKR_SHADER_PATH_NEE ? 1u : std::max(1u, points + area * b->n_light + s->env_n);
   b->nmat = nmat;
   b->nsets = sets;
   b->job_in.assign(jobs, jobs + njobs);

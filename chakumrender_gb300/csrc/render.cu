@@ -92,7 +92,8 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   for (const DevLight &L : s->host_lights) (L.type == CKR_LIGHT_POINT ? point_lights : area_lights)++;
   uint32_t per_path = cfg->shader == CKR_SHADER_PATH_NEE
                           ? 1u
-                          : point_lights + area_lights * prm.n_light + (cfg->shader == CKR_SHADER_DIRECT_MIS ? prm.n_brdf : 0);
+                          : point_lights + area_lights * prm.n_light + (cfg->shader == CKR_SHADER_DIRECT_MIS ? prm.n_brdf : 0) +
+                                (cfg->shader == CKR_SHADER_DIRECT_MIS || cfg->shader == CKR_SHADER_PATH ? s->env_n : 0);
   if (cfg->shader == CKR_SHADER_DIRECT_CV) per_path = mesh_lights_of(s) * prm.n_light;
   if (cfg->shader == CKR_SHADER_EXPLICIT) per_path = 0;  // the MISCV direct term traces no shadow rays
   prm.shadow_per_path = std::max(1u, per_path);
@@ -373,7 +374,8 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
   uint64_t per_path = cfg->shader == CKR_SHADER_PATH_NEE
                           ? 1u
                           : (uint64_t)point_lights + (uint64_t)area_lights * prm.n_light +
-                                (cfg->shader == CKR_SHADER_DIRECT_MIS ? prm.n_brdf : 0);
+                                (cfg->shader == CKR_SHADER_DIRECT_MIS ? prm.n_brdf : 0) +
+                                (cfg->shader == CKR_SHADER_DIRECT_MIS || cfg->shader == CKR_SHADER_PATH ? s->env_n : 0);
   if (cfg->shader == CKR_SHADER_DIRECT_CV) per_path = (uint64_t)mesh_lights_of(s) * prm.n_light;
   if (per_path > kNoAllocShadow) return CKR_ERR_TOO_LARGE;
   prm.shadow_per_path = (uint32_t)std::max<uint64_t>(1, per_path);

@@ -123,6 +123,70 @@ __device__ __forceinline__ F3 mat_radiance(const ShadeView &sv, uint32_t m) {
   return f3(mm.radiance[0], mm.radiance[1], mm.radiance[2]);
 }
 
+// ---- environment light (EnvSource, headers/lightSources.h:33-109) ----
+
+// World direction -> the map's frame: z along the up axis (EnvSource::getRadiance).
+__device__ __forceinline__ F3 env_local(uint32_t axis, F3 w) {
+  return axis == 0 ? f3(w.y, w.z, w.x) : axis == 1 ? f3(w.x, w.z, w.y) : w;
+}
+__device__ __forceinline__ F3 env_world(uint32_t axis, F3 l) {
+  return axis == 0 ? f3(l.z, l.x, l.y) : axis == 1 ? f3(l.x, l.z, l.y) : l;
+}
+
+// EnvSource::getThetaPhi + getRadiance's pixel: theta = acos z, phi from the
+// asin of the normalised (x, y) by quadrant, col = phi / 2pi * w, row = theta / pi
+// * h (clamped to the image; the reference indexes past it at phi = 2pi).
+__device__ __forceinline__ float4 env_lookup(const ShadeView &sv, F3 w) {
+  const F3 l = env_local(sv.env_axis, w);
+  const float z = fminf(1.0f, fmaxf(-1.0f, l.z));
+  const float theta = acosf(z);
+  const float st = sqrtf(fmaxf(0.f, 1.0f - z * z));
+  float phi = 0.f;
+  if (st >= 1e-12f) {
+    const float x = fminf(1.0f, fmaxf(-1.0f, l.x / st)), y = fminf(1.0f, fmaxf(-1.0f, l.y / st));
+    if (y >= 0.f && x >= 0.f) phi = asinf(y);
+    else if (y >= 0.f && x <= 0.f) phi = kPi - asinf(y);
+    else if (y <= 0.f && x <= 0.f) phi = kPi + asinf(-y);
+    else phi = 2.0f * kPi - asinf(-y);
+  }
+  uint32_t col = (uint32_t)(phi / (2.0f * kPi) * (float)sv.env_w);
+  uint32_t row = (uint32_t)(theta / kPi * (float)sv.env_h);
+  col = col < sv.env_w ? col : sv.env_w - 1;
+  row = row < sv.env_h ? row : sv.env_h - 1;
+  return __ldg(&sv.env[(size_t)row * sv.env_w + col]);
+}
+
+// Largest i in [0, n) with cdf[i] <= u (cdf[0] = 0 <= u < 1 = cdf[n]); rows or
+// columns of zero weight are never returned.
+__device__ __forceinline__ uint32_t env_search(const float *cdf, uint32_t n, float u) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(&cdf[mid]) <= u) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// A direction with density luminance(L) / A in solid angle: a row by the
+// marginal CDF (e0), a column by that row's CDF (e1), phi uniform across the
+// pixel (e1's remainder in its column), cos theta uniform across the row's band
+// (e2).
+__device__ __forceinline__ F3 env_sample(const ShadeView &sv, float e0, float e1, float e2) {
+  const uint32_t r = env_search(sv.env_marg, sv.env_h, e0);
+  const float *cr = sv.env_cond + (size_t)r * (sv.env_w + 1);
+  const uint32_t c = env_search(cr, sv.env_w, e1);
+  const float c0 = __ldg(&cr[c]), c1 = __ldg(&cr[c + 1]);
+  const float u = c1 > c0 ? fminf(fmaxf((e1 - c0) / (c1 - c0), 0.f), 1.0f) : 0.5f;
+  const float phi = ((float)c + u) * (2.0f * kPi / (float)sv.env_w);
+  const float ca = __ldg(&sv.env_cos[r]), cb = __ldg(&sv.env_cos[r + 1]);
+  const float ct = ca - e2 * (ca - cb);
+  const float st = sqrtf(fmaxf(0.f, 1.0f - ct * ct));
+  float sp, cp;
+  sincosf(phi, &sp, &cp);
+  return env_world(sv.env_axis, f3(st * cp, st * sp, ct));
+}
+
 // Result of testing one direction against every area/sphere light: the sum
 // sum_k N_k p_k(w) of the light techniques' pdfs (Pdf::pdfVal, src/mis.cpp:34-94)
 // and the nearest light surface the ray meets (its distance and radiance).
@@ -133,6 +197,9 @@ struct LightQuery {
   bool hit;
 };
 
+// ENV: the environment light takes part (pdf n_env luminance / A for every
+// direction; seen when no other light is met, src/lightSources.cpp:103-106).
+template <bool ENV = false>
 __device__ __forceinline__ LightQuery query_lights(const ShadeView &sv, F3 x, F3 o_off, F3 w, uint32_t n_per_light) {
   LightQuery q;
   q.pdf_sum = 0.f;
@@ -167,6 +234,15 @@ __device__ __forceinline__ LightQuery query_lights(const ShadeView &sv, F3 x, F3
         q.Le = mat_radiance(sv, sv.sph_mat[L.first]);
         q.hit = true;
       }
+    }
+  }
+  if (ENV && sv.env_n) {
+    const float4 e = env_lookup(sv, w);
+    q.pdf_sum += (float)sv.env_n * e.w * sv.env_inv_area;
+    if (!q.hit) {
+      q.hit = true;
+      q.d = 3.0e38f;
+      q.Le = f3(e.x, e.y, e.z);
     }
   }
   return q;

@@ -46,6 +46,13 @@ struct ShadeView {
   const float *pcdf;          // per-light triangle power CDFs (DevLight::pcdf)
   const float *sel_cdf;       // power CDF over the emitter lights [first_emit, first_emit + n_emit)
   uint32_t first_emit, n_emit;
+  // Environment light (ckr_env_light); env_n = 0 when there is none.
+  const float4 *env;         // per pixel: radiance rgb, luminance
+  const float *env_marg;     // env_h + 1: CDF over rows (luminance x solid angle)
+  const float *env_cond;     // env_h x (env_w + 1): CDF over the columns of each row
+  const float *env_cos;      // env_h + 1: cos(r pi / env_h)
+  uint32_t env_w, env_h, env_axis, env_n;
+  float env_inv_area;        // 1 / integral of the luminance over the sphere
 };
 
 }  // namespace ckr
@@ -69,6 +76,10 @@ struct ckr_scene {
   ckr::DevBuf<uint32_t> tri_light;
   ckr::DevBuf<float> pcdf, sel_cdf;
   uint32_t nlights = 0, first_point = 0, first_emit = 0, n_emit = 0;
+  ckr::DevBuf<float4> env;
+  ckr::DevBuf<float> env_marg, env_cond, env_cos;
+  uint32_t env_w = 0, env_h = 0, env_axis = 1, env_n = 0;
+  float env_inv_area = 0.f;
   float bounds[6] = {0, 0, 0, 0, 0, 0};  // scene box (lo.xyz, hi.xyz) of triangles and spheres
   std::vector<ckr_material> host_mats;
   std::vector<ckr::DevLight> host_lights;

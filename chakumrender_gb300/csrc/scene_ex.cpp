@@ -26,6 +26,15 @@ ShadeView shade_view_of(const ckr_scene *s) {
   v.sel_cdf = s->sel_cdf.ptr;
   v.first_emit = s->first_emit;
   v.n_emit = s->n_emit;
+  v.env = s->env.ptr;
+  v.env_marg = s->env_marg.ptr;
+  v.env_cond = s->env_cond.ptr;
+  v.env_cos = s->env_cos.ptr;
+  v.env_w = s->env_w;
+  v.env_h = s->env_h;
+  v.env_axis = s->env_axis;
+  v.env_n = s->env_n;
+  v.env_inv_area = s->env_inv_area;
   return v;
 }
 
@@ -54,6 +63,73 @@ double build_inv_cdf(const float *tri9, uint32_t first, uint32_t count, uint32_t
   }
   for (uint32_t i = last; i < kInvCdfBins; ++i) inv[i] = count - 1;
   return area;
+}
+
+// Tables of the environment light: per-pixel radiance and luminance, the row
+// CDF weighted by luminance x solid angle, each row's column CDF, and the band
+// boundaries' cosines.  Built in FP64, stored in FP32 with the last CDF entries 1.
+struct EnvTables {
+  std::vector<float4> px;
+  std::vector<float> marg, cond, cosr;
+  double area = 0;
+};
+
+int build_env(const ckr_env_light &e, EnvTables &t) {
+  const uint32_t w = e.width, h = e.height;
+  if (!e.rgb || w == 0 || h == 0 || (uint64_t)w * h > (1ull << 28) || e.axis > 2 || e.n_samples > 256)
+    return CKR_ERR_INVALID_ARGUMENT;
+  // BaseSource: the colour divided by its largest component (Vec::maxnorm), times
+  // the intensity.
+  double c[3] = {e.color[0], e.color[1], e.color[2]};
+  double mx = c[0];
+  if (mx < c[1]) mx = c[1];
+  if (mx < c[2]) mx = c[2];
+  if (!(mx > 0) || !std::isfinite(mx) || !std::isfinite((double)e.intensity)) return CKR_ERR_INVALID_ARGUMENT;
+  for (int k = 0; k < 3; ++k) c[k] = c[k] / mx * e.intensity;
+  t.px.resize((size_t)w * h);
+  t.cosr.resize(h + 1);
+  for (uint32_t r = 0; r <= h; ++r) t.cosr[r] = (float)std::cos(M_PI * r / h);
+  t.cosr[0] = 1.0f;
+  t.cosr[h] = -1.0f;
+  std::vector<double> rowsum(h, 0.0), lum((size_t)w * h);
+  for (uint32_t r = 0; r < h; ++r)
+    for (uint32_t col = 0; col < w; ++col) {
+      const size_t i = (size_t)r * w + col;
+      double L[3];
+      for (int k = 0; k < 3; ++k) {
+        L[k] = (double)e.rgb[3 * i + k] * c[k];
+        if (!std::isfinite(L[k])) return CKR_ERR_INVALID_ARGUMENT;
+      }
+      double g = L[0] * 0.3 + L[1] * 0.59 + L[2] * 0.11;  // to_greyScale
+      lum[i] = g > 0 ? g : 0.0;
+      t.px[i] = make_float4((float)L[0], (float)L[1], (float)L[2], (float)lum[i]);
+      rowsum[r] += lum[i];
+    }
+  const double dphi = 2.0 * M_PI / w;
+  std::vector<double> band(h);
+  for (uint32_t r = 0; r < h; ++r) {
+    band[r] = (std::cos(M_PI * r / h) - std::cos(M_PI * (r + 1) / h)) * dphi;  // solid angle of one pixel
+    t.area += rowsum[r] * band[r];
+  }
+  if (!(t.area > 0)) return CKR_ERR_INVALID_ARGUMENT;  // a black environment cannot be sampled
+  t.marg.resize(h + 1);
+  t.cond.resize((size_t)h * (w + 1));
+  double run = 0;
+  t.marg[0] = 0.f;
+  for (uint32_t r = 0; r < h; ++r) {
+    run += rowsum[r] * band[r];
+    t.marg[r + 1] = (float)(run / t.area);
+    float *cr = &t.cond[(size_t)r * (w + 1)];
+    double cr_run = 0;
+    cr[0] = 0.f;
+    for (uint32_t col = 0; col < w; ++col) {
+      cr_run += lum[(size_t)r * w + col];
+      cr[col + 1] = rowsum[r] > 0 ? (float)(cr_run / rowsum[r]) : (float)(col + 1) / (float)w;
+    }
+    cr[w] = 1.0f;
+  }
+  t.marg[h] = 1.0f;
+  return CKR_OK;
 }
 
 template <typename T>
@@ -153,6 +229,11 @@ extern "C" int ckr_scene_create_ex(const ckr_scene_desc *d, ckr_scene **out) {
     sel_cdf[k - first_emit] = total > 0 ? (float)(run / total) : (float)(k - first_emit + 1) / (float)n_emit;
   }
   if (n_emit) sel_cdf.back() = 1.0f;
+  EnvTables env;
+  if (d->env) {
+    const int es = build_env(*d->env, env);
+    if (es != CKR_OK) return es;
+  }
   ckr_scene *s = nullptr;
   int st = ckr_scene_create(d->tri9, d->ntri, d->sph4, d->nsph, &d->build, &s);
   if (st != CKR_OK) return st;
@@ -166,9 +247,20 @@ extern "C" int ckr_scene_create_ex(const ckr_scene_desc *d, ckr_scene **out) {
       (st = upload(s->cdf, cdf.data(), cdf.size())) != CKR_OK ||
       (st = upload(s->tri_light, tri_light.data(), tri_light.size())) != CKR_OK ||
       (st = upload(s->pcdf, pcdf.data(), pcdf.size())) != CKR_OK ||
-      (st = upload(s->sel_cdf, sel_cdf.data(), sel_cdf.size())) != CKR_OK) {
+      (st = upload(s->sel_cdf, sel_cdf.data(), sel_cdf.size())) != CKR_OK ||
+      (st = upload(s->env, env.px.data(), env.px.size())) != CKR_OK ||
+      (st = upload(s->env_marg, env.marg.data(), env.marg.size())) != CKR_OK ||
+      (st = upload(s->env_cond, env.cond.data(), env.cond.size())) != CKR_OK ||
+      (st = upload(s->env_cos, env.cosr.data(), env.cosr.size())) != CKR_OK) {
     ckr_scene_destroy(s);
     return st;
+  }
+  if (d->env) {
+    s->env_w = d->env->width;
+    s->env_h = d->env->height;
+    s->env_axis = d->env->axis;
+    s->env_n = d->env->n_samples ? d->env->n_samples : 10;  // MIS::nEnMpIS
+    s->env_inv_area = (float)(1.0 / env.area);
   }
   s->nlights = d->nlights;
   s->first_point = first_point;

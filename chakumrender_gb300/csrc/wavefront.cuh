@@ -282,7 +282,7 @@ __device__ uint32_t light_samples(const ShadeView &sv, const Params &prm, const 
       F3 w = sample_light(sv, L, S.x, e0, e1, e2);
       float c = dot(w, S.n);
       if (c < 0.f) continue;
-      LightQuery lq = query_lights(sv, S.x, o_off, w, prm.n_light);
+      LightQuery lq = query_lights<true>(sv, S.x, o_off, w, prm.n_light);
       if (!lq.hit) continue;
       if (write) {
         float denom = lq.pdf_sum + (float)prm.n_brdf * pdf_eval(M, S.n, S.wo_ref, S.wo, w);
@@ -295,6 +295,27 @@ __device__ uint32_t light_samples(const ShadeView &sv, const Params &prm, const 
       ++cnt;
     }
   }
+  // Environment light: its own technique after the area lights (EnMpIS of
+  // MIS::getSamples, src/mis.cpp:154-166).
+  for (uint32_t i = 0; i < sv.env_n; ++i, ++sidx) {
+    float e0 = ckr_draw_f(key, ctr(sample, depth, 3 * sidx));
+    float e1 = ckr_draw_f(key, ctr(sample, depth, 3 * sidx + 1));
+    float e2 = ckr_draw_f(key, ctr(sample, depth, 3 * sidx + 2));
+    F3 w = env_sample(sv, e0, e1, e2);
+    float c = dot(w, S.n);
+    if (c < 0.f) continue;
+    LightQuery lq = query_lights<true>(sv, S.x, o_off, w, prm.n_light);
+    if (!lq.hit) continue;
+    if (write) {
+      float denom = lq.pdf_sum + (float)prm.n_brdf * pdf_eval(M, S.n, S.wo_ref, S.wo, w);
+      float f = brdf_eval(M, S.n, S.wo_ref, S.wo, w);
+      F3 contrib = mulc(beta, mulc(fcol, lq.Le)) * (f * c / (denom + 1e-20f));
+      so[cnt] = make_float4(o_off.x, o_off.y, o_off.z, 0.f);
+      sd[cnt] = make_float4(w.x, w.y, w.z, shadow_tmax(lq.d));
+      sc[cnt] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
+    }
+    ++cnt;
+  }
   if (DETERMINISTIC_SPLIT) {
     // BRDF technique of MIS::getSamples: N*spec lobe samples, the rest cosine
     // (MaterialType::getBrdfDirectionSamples, src/materialTypes.cpp:118-134).
@@ -305,7 +326,7 @@ __device__ uint32_t light_samples(const ShadeView &sv, const Params &prm, const 
       F3 w = i < nlobe ? sample_lobe(M, S.n, S.wo_ref, S.wo, e1, e2) : sample_cosine(S.n, e1, e2);
       float c = dot(w, S.n);
       if (c < 0.f) continue;
-      LightQuery lq = query_lights(sv, S.x, o_off, w, prm.n_light);
+      LightQuery lq = query_lights<true>(sv, S.x, o_off, w, prm.n_light);
       if (!lq.hit) continue;
       if (write) {
         float denom = lq.pdf_sum + (float)nb * pdf_eval(M, S.n, S.wo_ref, S.wo, w);
@@ -435,6 +456,12 @@ __global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params pr
       meta = P.meta[slot];
       pc = path_ctx(prm, meta.w);
       sv.mats = sv0.mats + pc.mat_off;
+      if (id == kMiss && SHADER == CKR_SHADER_PATH && sv.env_n && meta.z > 0) {
+        // A BRDF-sampled ray left the scene: the environment, with its MIS weight.
+        const float4 rd = P.ray_d[slot], b4 = P.beta[slot];
+        const float4 e = env_lookup(sv, f3(rd.x, rd.y, rd.z));
+        add_px(P.accum, meta.x, mulc(f3(b4.x, b4.y, b4.z), f3(e.x, e.y, e.z)) * b4.w);
+      }
       if (id != kMiss) {
         float4 ro = P.ray_o[slot], rd = P.ray_d[slot], b4 = P.beta[slot];
         beta = f3(b4.x, b4.y, b4.z);
@@ -596,7 +623,7 @@ __global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params pr
         float pb = pdf_eval(M, S.n, S.wo_ref, S.wo, w);
         float f = brdf_eval(M, S.n, S.wo_ref, S.wo, w);
         if (pb > 0.f && f > 0.f) {
-          LightQuery lq = query_lights(sv, S.x, o_off, w, prm.n_light);
+          LightQuery lq = query_lights<true>(sv, S.x, o_off, w, prm.n_light);
           float wb = (float)prm.n_brdf * pb / ((float)prm.n_brdf * pb + lq.pdf_sum);
           F3 nb = mulc(beta, fcol) * (f * c / (pb * (1.0f - prm.rr_prob)));
           cont = true;

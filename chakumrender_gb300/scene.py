@@ -33,9 +33,15 @@ class Light(C.Structure):
                 ("pad", C.c_float)]
 
 
+class EnvLight(C.Structure):
+    _fields_ = [("rgb", P), ("width", U32), ("height", U32), ("axis", U32), ("color", F3), ("intensity", C.c_float),
+                ("n_samples", U32)]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [("tri9", P), ("tri_material", P), ("ntri", U32), ("sph4", P), ("sph_material", P), ("nsph", U32),
-                ("materials", P), ("nmaterials", U32), ("lights", P), ("nlights", U32), ("build", BuildParams)]
+                ("materials", P), ("nmaterials", U32), ("lights", P), ("nlights", U32), ("build", BuildParams),
+                ("env", C.POINTER(EnvLight))]
 
 
 class Camera(C.Structure):
@@ -75,7 +81,7 @@ def render_cfg(shader=SHADER_PATH, spp=16, max_depth=4, n_light=1, n_brdf=1, rr_
 class SceneData:
     """Host-side scene description (arrays kept alive for the descriptor)."""
 
-    def __init__(self, tri9, tri_mat, sph4, sph_mat, materials, lights, camera: Camera | None = None):
+    def __init__(self, tri9, tri_mat, sph4, sph_mat, materials, lights, camera: Camera | None = None, env=None):
         self.tri9 = np.ascontiguousarray(tri9, np.float32).reshape(-1, 9)
         self.tri_mat = np.ascontiguousarray(tri_mat, np.uint32)
         self.sph4 = np.ascontiguousarray(sph4, np.float32).reshape(-1, 4)
@@ -91,13 +97,22 @@ class SceneData:
             self.lights = (Light * max(1, len(lights)))(*lights)
             self.nlights = len(lights)
         self.camera = camera
+        self.env = None
+        if env is not None:
+            self.set_env(*env) if isinstance(env, tuple) else self.set_env(**env)
+
+    def set_env(self, image, axis: int = 1, color=(1.0, 1.0, 1.0), intensity: float = 1.0, n_samples: int = 0):
+        """Environment light (ckr_env_light): image (h, w, 3) equirectangular about `axis`."""
+        self.env_image = np.ascontiguousarray(image, np.float32).reshape(image.shape[0], image.shape[1], 3)
+        h, w = self.env_image.shape[:2]
+        self.env = EnvLight(_ptr(self.env_image), w, h, axis, F3(*color), intensity, n_samples)
 
     def desc(self, max_leaf: int = 0) -> SceneDesc:
         return SceneDesc(_ptr(self.tri9) if len(self.tri9) else None, _ptr(self.tri_mat) if len(self.tri9) else None,
                          len(self.tri9), _ptr(self.sph4) if len(self.sph4) else None,
                          _ptr(self.sph_mat) if len(self.sph4) else None, len(self.sph4),
                          C.addressof(self.materials), self.nmat, C.addressof(self.lights), self.nlights,
-                         BuildParams(max_leaf, 0, 0))
+                         BuildParams(max_leaf, 0, 0), C.pointer(self.env) if self.env is not None else None)
 
 
 def load_xml(path) -> SceneData:

@@ -160,6 +160,31 @@ typedef struct ckr_light {
   float pad;
 } ckr_light;
 
+/* Environment light (EnvSource, headers/lightSources.h:33-109, attached by
+ * LightSource::addESource; the reference's call, src/prepareScene.cpp:149-153, is
+ * commented out and its image env1.ppm is missing).  An equirectangular RGB image
+ * about the up axis: row r covers theta in [r, r + 1) pi / height, column c covers
+ * phi in [c, c + 1) 2 pi / width, looked up as EnvSource::getRadiance does; the
+ * radiance is image x color / max(color) x intensity (BaseSource).  Directions are
+ * sampled in proportion to the luminance 0.3 r + 0.59 g + 0.11 b (to_greyScale)
+ * over the sphere, with pdf(w) = luminance(L(w)) / A, A the luminance integral
+ * (EnvSource::calcArea, computed exactly here and numerically there).
+ * CKR_SHADER_DIRECT_MIS draws n_samples environment samples per point (MIS::nEnMpIS,
+ * default 10) into the MIS set, and a sample direction that meets no other light
+ * sees the environment when unoccluded (src/lightSources.cpp:103-106);
+ * CKR_SHADER_PATH does the same at every vertex, and its BRDF-sampled rays that
+ * leave the scene see the environment with their MIS weight.  The other shaders
+ * ignore it, as the reference's analytic (LTC) estimators do; camera rays that
+ * leave the scene are black, as in the reference. */
+typedef struct ckr_env_light {
+  const float *rgb;  /* width x height x 3 floats, host memory, read at scene creation */
+  uint32_t width, height;
+  uint32_t axis;     /* up axis: 0 x, 1 y, 2 z (EnvSource::axis) */
+  float color[3];
+  float intensity;
+  uint32_t n_samples; /* 0: 10 */
+} ckr_env_light;
+
 typedef struct ckr_scene_desc {
   const float *tri9;            /* ntri x (A, B, C), emitter triangles included */
   const uint32_t *tri_material; /* ntri material indices (NULL: all 0) */
@@ -172,6 +197,7 @@ typedef struct ckr_scene_desc {
   const ckr_light *lights;
   uint32_t nlights;
   ckr_build_params build;
+  const ckr_env_light *env;     /* NULL: no environment light */
 } ckr_scene_desc;
 
 /* Scene with shading data (prepareObjects + prepareLightSources + loadAccels +

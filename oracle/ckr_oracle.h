@@ -114,6 +114,12 @@ struct ckr_render_cfg;
 void orc_render(const struct ckr_scene_desc *desc, const struct ckr_camera *cam, const struct ckr_render_cfg *cfg,
                 double *rgb, int threads);
 
+/* Environment light (EnvSource restated): radiance + luminance per direction and
+ * the luminance integral; directions drawn from uniforms (3 per sample). */
+struct ckr_env_light;
+void orc_env_eval(const struct ckr_env_light *e, const double *dirs, uint32_t n, double *rgbl, double *area);
+void orc_env_sample(const struct ckr_env_light *e, const double *u, uint32_t n, double *dirs);
+
 /* ---------------------------------------------------------------------- */
 /* Learned light-selection network (orc_mlp.c; no reference counterpart).  */
 /* ---------------------------------------------------------------------- */

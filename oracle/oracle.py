@@ -295,3 +295,45 @@ def render(scene_data, cam, cfg, threads: int = 0) -> np.ndarray:
     out = np.empty((cam.height, cam.width, 3), np.float64)
     L.orc_render(C.byref(d), C.byref(cam), C.byref(cfg), _p(out), threads)
     return out
+
+
+def env_eval(env, dirs):
+    """The oracle's environment lookup: (n, 4) radiance rgb + luminance, and the
+    luminance integral A.  `env` is a chakumrender_gb300.scene.EnvLight."""
+    L = orc()
+    if not hasattr(L, "_env"):
+        _sig(L, "orc_env_eval", [P, P, U32, P, P], None)
+        _sig(L, "orc_env_sample", [P, P, U32, P], None)
+        L._env = True
+    dirs = np.ascontiguousarray(dirs, np.float64).reshape(-1, 3)
+    out = np.empty((len(dirs), 4), np.float64)
+    area = C.c_double()
+    L.orc_env_eval(C.byref(env), _p(dirs), len(dirs), _p(out), C.byref(area))
+    return out, area.value
+
+
+def env_sample(env, u):
+    """Directions drawn by the oracle's environment sampler from uniforms u (n, 3)."""
+    env_eval(env, np.zeros((0, 3)))  # signatures
+    u = np.ascontiguousarray(u, np.float64).reshape(-1, 3)
+    out = np.empty((len(u), 3), np.float64)
+    orc().orc_env_sample(C.byref(env), _p(u), len(u), _p(out))
+    return out
+
+
+def ref_env(image, axis, color, intensity, dirs, nsamples=0):
+    """The reference's EnvSource: getRadiance per direction, normalizationArea, and
+    the first nsamples of its importance-sampled directions."""
+    L = ref()
+    if not hasattr(L, "_env"):
+        _sig(L, "ref_env", [P, U32, U32, U32, P, C.c_double, P, U32, P, P, P, U32])
+        L._env = True
+    img = np.ascontiguousarray(image, np.float64)
+    h, w = img.shape[:2]
+    dirs = np.ascontiguousarray(dirs, np.float64).reshape(-1, 3)
+    col = np.ascontiguousarray(color, np.float64)
+    rgb = np.empty((len(dirs), 3), np.float64)
+    area = C.c_double()
+    smp = np.empty((max(nsamples, 1), 3), np.float64)
+    L.ref_env(_p(img), w, h, axis, _p(col), intensity, _p(dirs), len(dirs), _p(rgb), C.byref(area), _p(smp), nsamples)
+    return rgb, area.value, smp[:nsamples]

@@ -259,3 +259,35 @@ int ref_write_image(const char *dir, const double *rgb, uint32_t w, uint32_t h) 
 }
 
 }  // extern "C"
+
+// ---- environment light: EnvSource (headers/lightSources.h:33-109) -------------
+extern "C" {
+
+// Builds EnvSource(image, w, h, axis, colour, intensity) -- whose constructor runs
+// initSamples: the numeric normalisation area and the 200,000 importance-sampled
+// directions -- then returns getRadiance for n directions, the area, and up to
+// nsamp of its sampled directions.
+int ref_env(const double *img, uint32_t w, uint32_t h, uint32_t axis, const double *col, double intensity,
+            const double *dirs, uint32_t n, double *rgb, double *area, double *samples, uint32_t nsamp) {
+  std::vector<Vec> image((size_t)w * h);
+  for (size_t i = 0; i < image.size(); ++i) image[i] = Vec(img[3 * i], img[3 * i + 1], img[3 * i + 2]);
+  EnvSource *e = new EnvSource(image.data(), w, h, axis, Vec(col[0], col[1], col[2]), intensity);
+  for (uint32_t i = 0; i < n; ++i) {
+    Vec L = e->getRadiance(Vec(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]));
+    rgb[3 * i] = L.x;
+    rgb[3 * i + 1] = L.y;
+    rgb[3 * i + 2] = L.z;
+  }
+  *area = e->normalizationArea;
+  const uint32_t total = EnvSource::nSamples * EnvSource::multiplier;
+  for (uint32_t i = 0; i < nsamp && i < total; ++i) {
+    samples[3 * i] = e->impSamples[i].x;
+    samples[3 * i + 1] = e->impSamples[i].y;
+    samples[3 * i + 2] = e->impSamples[i].z;
+  }
+  delete[] e->envMap;
+  delete e;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,54 @@
+"""Environment light on the GPU (ckr_env_light through ckr_render): against the FP64
+oracle with the same random streams, and against the exact radiance of a plane."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle as O
+from chakumrender_gb300 import scene as S
+from scene_io import rel_mse
+from test_env_light import COLOR, INTENSITY, env_image, exact_plane_radiance, plane_scene
+
+pytestmark = pytest.mark.gpu
+BOX = S.SCENES / "box.xml"
+
+
+# (shader, spp, n_brdf, max_depth, env samples, relMSE bar, bar with the 1 % worst
+# pixel terms left out).  Both sides draw the same random numbers.  Direct light
+# agrees everywhere; in the path tracer the rare paths that FP32 and FP64 send to
+# different surfaces now leave through the open front of the box and see the bright
+# "sun" pixel of the map, so the bar is on the trimmed relMSE and the mean.
+@pytest.mark.parametrize("shader,spp,nb,depth,ne,bar,tbar", [
+    (S.SHADER_DIRECT_MIS, 4, 20, 1, 4, 1e-4, 1e-5),
+    (S.SHADER_PATH, 16, 1, 4, 1, 1e-2, 1e-3),
+])
+def test_box_with_environment_vs_oracle(torch_cuda, shader, spp, nb, depth, ne, bar, tbar):
+    sd = S.load_xml(BOX)
+    sd.set_env(env_image(), axis=1, color=COLOR, intensity=INTENSITY, n_samples=ne)
+    cam = sd.camera
+    cam.width = cam.height = 128
+    cfg = S.render_cfg(shader=shader, spp=spp, n_light=4, n_brdf=nb, max_depth=depth)
+    g = S.RenderScene(sd).render_host(cam, cfg).astype(np.float64)
+    o = O.render(sd, cam, cfg)
+    e = rel_mse(g, o)
+    terms = np.sort(((g - o) ** 2 / (o * o + 1e-2)).ravel())
+    trimmed = terms[: int(0.99 * terms.size)].mean()
+    print(f"shader {shader} with environment: relMSE vs oracle {e:.3e}, trimmed {trimmed:.3e}, "
+          f"mean {g.mean():.5f} vs {o.mean():.5f}")
+    assert np.all(np.isfinite(g)) and g.min() >= 0
+    assert e <= bar and trimmed <= tbar
+    assert abs(g.mean() - o.mean()) <= 2e-3 * o.mean()
+
+
+@pytest.mark.parametrize("shader", [S.SHADER_DIRECT_MIS, S.SHADER_PATH])
+def test_plane_under_environment_is_unbiased(torch_cuda, shader):
+    img = env_image()
+    sd, cam = plane_scene(img)
+    cam.width = cam.height = 64
+    cfg = S.render_cfg(shader=shader, spp=256, max_depth=2, n_light=1, n_brdf=4 if shader == S.SHADER_DIRECT_MIS else 1)
+    rgb = S.RenderScene(sd).render_host(cam, cfg).astype(np.float64).reshape(-1, 3)
+    mean, want = rgb.mean(0), exact_plane_radiance(img)
+    err = rgb.std(0) / np.sqrt(len(rgb))
+    print(f"shader {shader}: plane radiance {mean} vs exact {want} (+- {err})")
+    assert np.all(np.abs(mean - want) < 5 * err + 2e-3 * want)

@@ -270,7 +270,7 @@ def bench_manylight(torch):
     uniform per triangle in [0.1, 0.8], 10^3 room, 4,096 emissive triangles in 64
     clusters), 1920x1080, 64 spp, max depth 6, one-sample NEE path tracer.  Plain =
     lights chosen in proportion to power; learned = the proposal network (BF16
-    tensor-core MLP, defensive 0.2, Adam 1e-3) trained online from scratch inside
+    tensor-core MLP, defensive 0.2, Adam 3e-3) trained online from scratch inside
     the timed frame (cold) or carried over from one earlier frame (warm).  relMSE is
     taken over a 320x180 window of the frame against a 16,384-spp FP64-accumulated
     render of that window; the learned frame gets the spp that fit in the plain
@@ -312,7 +312,7 @@ def bench_manylight(torch):
     t_plain = timed(lambda: scene.render(cam, cfg(SPP, 2), rgb.data_ptr()))
     closest, shadow = scene.ray_stats(reset=True)
     e_plain = rel_mse()
-    opts = dict(minibatch=4096, max_steps=1000)
+    opts = dict(minibatch=4096, max_steps=1000, lr=3e-3)
     cold = Proposal(scene, seed=1, **opts)
     t_cold64 = timed(lambda: cold.render(cam, cfg(SPP, 3), rgb.data_ptr()))
     e_cold64 = rel_mse()
@@ -345,7 +345,7 @@ def bench_manylight(torch):
             "reference": {"spp": 16384, "window": [X0, Y0, CW, CH], "sec": round(ref_sec, 2),
                           "accumulation": "fp64"},
             "proposal": {"minibatch": opts["minibatch"], "max_steps": opts["max_steps"], "defensive": 0.2,
-                         "lr": 1e-3}}
+                         "lr": opts["lr"]}}
 
 
 def bench_batch(torch):

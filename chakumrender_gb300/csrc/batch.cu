@@ -148,7 +148,7 @@ int enqueue(ckr_batch *b, JobSet &set, bool pack, size_t wave, cudaStream_t stre
   const int g_ext = grid_for((const void *)extend_fn, smem, TPB);
   const int g_sh = grid_for((const void *)shadow_fn, smem, TPB);
   const bool nee = b->shader == CKR_SHADER_PATH_NEE;
-  const int g_shade = grid_for(nee ? (const void *)k_shade_nee<TPB> : (const void *)k_shade<CKR_SHADER_PATH, TPB>,
+  const int g_shade = grid_for(nee ? (const void *)k_shade_nee<TPB> : (const void *)k_shade_path<TPB>,
                                0, TPB);
   Params prm{};
   prm.shader = b->shader;
@@ -187,7 +187,7 @@ int enqueue(ckr_batch *b, JobSet &set, bool pack, size_t wave, cudaStream_t stre
         CKR_CUDA_TRY(cudaMemsetAsync(P.counts + (cur ^ 1), 0, sizeof(uint32_t), stream));
         CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), stream));
         if (nee) k_shade_nee<TPB><<<g_shade, TPB, 0, stream>>>(shv, P, prm, cur, Learn{});
-        else k_shade<CKR_SHADER_PATH, TPB><<<g_shade, TPB, 0, stream>>>(shv, P, prm, cur, (int)d, nullptr);
+        else k_shade_path<TPB><<<g_shade, TPB, 0, stream>>>(shv, P, prm, cur, (int)d, nullptr);
         shadow_fn<<<g_sh, TPB, smem, stream>>>(sv, P, depth, cur, nullptr);
         n_launch += 3;
         cur ^= 1;

@@ -174,7 +174,7 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const void *shade_fn = cfg->shader == CKR_SHADER_EXPLICIT ? (const void *)k_shade<CKR_SHADER_EXPLICIT, kRTPB>
                          : cfg->shader == CKR_SHADER_PATH_NEE ? (const void *)k_shade_nee<kRTPB>
-                         : cfg->shader == CKR_SHADER_PATH      ? (const void *)k_shade<CKR_SHADER_PATH, kRTPB>
+                         : cfg->shader == CKR_SHADER_PATH      ? (const void *)k_shade_path<kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_CV  ? (const void *)k_shade<CKR_SHADER_DIRECT_CV, kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_MIS ? (const void *)k_shade<CKR_SHADER_DIRECT_MIS, kRTPB>
                                                                 : (const void *)k_shade<CKR_SHADER_DIRECT_MISCV, kRTPB>;
@@ -216,7 +216,7 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
       else if (cfg->shader == CKR_SHADER_PATH_NEE)
         k_shade_nee<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, lr);
       else if (cfg->shader == CKR_SHADER_PATH)
-        k_shade<CKR_SHADER_PATH, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
+        k_shade_path<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else if (cfg->shader == CKR_SHADER_DIRECT_CV)
         k_shade<CKR_SHADER_DIRECT_CV, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else if (cfg->shader == CKR_SHADER_DIRECT_MIS)
@@ -432,7 +432,7 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
   const int g_ext = grid_for((const void *)extend_fn, smem, kRTPB);
   const int g_sh = grid_for((const void *)shadow_fn, smem, kRTPB);
   const void *shade_fn = cfg->shader == CKR_SHADER_PATH_NEE ? (const void *)k_shade_nee<kRTPB>
-                         : cfg->shader == CKR_SHADER_PATH      ? (const void *)k_shade<CKR_SHADER_PATH, kRTPB>
+                         : cfg->shader == CKR_SHADER_PATH      ? (const void *)k_shade_path<kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_CV  ? (const void *)k_shade<CKR_SHADER_DIRECT_CV, kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_MIS ? (const void *)k_shade<CKR_SHADER_DIRECT_MIS, kRTPB>
                                                                 : (const void *)k_shade<CKR_SHADER_DIRECT_MISCV, kRTPB>;
@@ -450,7 +450,7 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
       if (cfg->shader == CKR_SHADER_PATH_NEE)
         k_shade_nee<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, Learn{});
       else if (cfg->shader == CKR_SHADER_PATH)
-        k_shade<CKR_SHADER_PATH, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
+        k_shade_path<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else if (cfg->shader == CKR_SHADER_DIRECT_CV)
         k_shade<CKR_SHADER_DIRECT_CV, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else if (cfg->shader == CKR_SHADER_DIRECT_MIS)

@@ -425,9 +425,8 @@ __device__ uint32_t cv_samples(const ShadeView &sv, const Params &prm, const Sur
 constexpr uint32_t kDimHemi = 1004, kExplicitTries = 8;
 
 template <uint32_t SHADER, int TPB>
-__global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params prm, int cur, int depth,
-                                                 const LtcEntry *__restrict__ ltc, SceneView scene = SceneView{},
-                                                 int stack_depth = 0) {
+__device__ __forceinline__ void shade(ShadeView sv0, Paths P, Params prm, int cur, int depth,
+                                      const LtcEntry *__restrict__ ltc, SceneView scene, int stack_depth) {
   const uint32_t n = P.counts[cur];
   const uint32_t *q = cur ? P.q1 : P.q0;
   uint32_t *qn = cur ? P.q0 : P.q1;
@@ -647,6 +646,24 @@ __global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params pr
   }
 }
 
+// Shading kernels.  The MIS path tracer's vertex is register hungry but short: at
+// 640 / TPB resident blocks (96 registers at 128 threads, with some spills) the box
+// frame took 1.50 ms against 1.65 ms at the default 149 registers.  The direct-light
+// shaders keep the compiler's choice (the MISCV shader at 188 spill-free registers was
+// 38 % slower than at its default 128).
+template <uint32_t SHADER, int TPB>
+__global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params prm, int cur, int depth,
+                                                 const LtcEntry *__restrict__ ltc, SceneView scene = SceneView{},
+                                                 int stack_depth = 0) {
+  shade<SHADER, TPB>(sv0, P, prm, cur, depth, ltc, scene, stack_depth);
+}
+
+template <int TPB>
+__global__ void __launch_bounds__(TPB, (640 / TPB > 1 ? 640 / TPB : 1))
+    k_shade_path(ShadeView sv0, Paths P, Params prm, int cur, int depth, const LtcEntry *__restrict__ ltc) {
+  shade<CKR_SHADER_PATH, TPB>(sv0, P, prm, cur, depth, ltc, SceneView{}, 0);
+}
+
 // CKR_SHADER_PATH_NEE: one light sample and one BRDF sample per vertex over many
 // lights.  The light technique draws an emitter light from the selection
 // distribution, one of its triangles in proportion to power and a uniform point
@@ -654,7 +671,8 @@ __global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params pr
 // weighted at the next vertex with the light technique's pdf of the previous
 // vertex (its pdf is carried in beta.w).  Balance heuristic throughout.
 template <int TPB>
-__global__ void __launch_bounds__(TPB) k_shade_nee(ShadeView sv0, Paths P, Params prm, int cur, Learn lr) {
+__global__ void __launch_bounds__(TPB, (640 / TPB > 1 ? 640 / TPB : 1))
+    k_shade_nee(ShadeView sv0, Paths P, Params prm, int cur, Learn lr) {
   const uint32_t n = P.counts[cur];
   const uint32_t *q = cur ? P.q1 : P.q0;
   uint32_t *qn = cur ? P.q0 : P.q1;

@@ -217,23 +217,36 @@ struct SmemInfer {
   int abort[kGroups];
 };
 
-// Network input of one row: a 12-float record, or (PATHS) the shading point of
-// queue entry `row` of the renderer (zeros where the entry is not a shaded surface).
-template <bool PATHS>
-__device__ __forceinline__ void load_row(const float4 *rec, const PathRows &pr, uint32_t row, float4 &r0, float4 &r1,
+// A queue entry's path state, gathered in two dependent steps (the path slot from the
+// queue, then the slot's hit and ray) so that each step's latency can overlap other
+// work of the tile before it.
+struct PathGather {
+  uint32_t slot, id, flags;
+  float4 ro, rd;
+  float t;
+};
+
+__device__ __forceinline__ void gather_slot(const PathRows &pr, uint32_t row, uint32_t n, PathGather &g) {
+  g.slot = row < n ? pr.queue[row] : 0xFFFFFFFFu;
+}
+
+__device__ __forceinline__ void gather_hit(const PathRows &pr, PathGather &g) {
+  g.id = kMiss;
+  if (g.slot == 0xFFFFFFFFu) return;
+  g.id = pr.hit_id[g.slot];
+  g.flags = pr.meta[g.slot].w;
+  g.ro = pr.ray_o[g.slot];
+  g.rd = pr.ray_d[g.slot];
+  g.t = pr.hit_t[g.slot];
+}
+
+// Network input of a gathered queue entry: its shading point (zeros where the entry is
+// not a shaded surface).
+__device__ __forceinline__ void path_row(const PathRows &pr, const PathGather &g, float4 &r0, float4 &r1,
                                          float4 &r2) {
   r0 = r1 = r2 = make_float4(0, 0, 0, 0);
-  if (!PATHS) {
-    r0 = rec[3 * (size_t)row];
-    r1 = rec[3 * (size_t)row + 1];
-    r2 = rec[3 * (size_t)row + 2];
-    return;
-  }
-  const uint32_t slot = pr.queue[row], id = pr.hit_id[slot];
-  const uint4 meta = pr.meta[slot];
-  if (id == kMiss || (meta.w & 1u)) return;
-  const float4 ro = pr.ray_o[slot], rd = pr.ray_d[slot];
-  Surface S = make_surface(pr.sv, f3(ro.x, ro.y, ro.z), f3(rd.x, rd.y, rd.z), id, pr.hit_t[slot]);
+  if (g.id == kMiss || (g.flags & 1u)) return;
+  Surface S = make_surface(pr.sv, f3(g.ro.x, g.ro.y, g.ro.z), f3(g.rd.x, g.rd.y, g.rd.z), g.id, g.t);
   const ckr_material &mm = pr.sv.mats[S.mat];
   if (mm.light_type != 0) return;
   r0 = make_float4(S.x.x, S.x.y, S.x.z, mm.alpha);
@@ -267,10 +280,26 @@ __global__ void __launch_bounds__(kInferTPB) k_mlp_infer(const float4 *__restric
   uint8_t *A = S.a[g];
   const uint32_t a_addr = tc::smem_u32(A), w_addr = tc::smem_u32(S.w);
   uint32_t phase = 0;
-  for (uint32_t tile = blockIdx.x * kGroups + g; tile * 128u < n; tile += gridDim.x * kGroups) {
+  const uint32_t stride = gridDim.x * kGroups;
+  // PATHS: the gather of the next tile's rows runs one tile ahead -- its queue load
+  // during this tile's MMA chain, its hit and ray loads during this tile's softmax --
+  // leaving only the triangle and material loads of make_surface exposed.
+  PathGather cur{}, nxt{};
+  if (PATHS) {
+    gather_slot(pr, (blockIdx.x * kGroups + g) * 128u + t, n, cur);
+    gather_hit(pr, cur);
+  }
+  for (uint32_t tile = blockIdx.x * kGroups + g; tile * 128u < n; tile += stride) {
     const uint32_t row = tile * 128u + t;
     float4 r0 = make_float4(0, 0, 0, 0), r1 = r0, r2 = r0;
-    if (row < n) load_row<PATHS>(rec, pr, row, r0, r1, r2);
+    if (PATHS) {
+      path_row(pr, cur, r0, r1, r2);
+      gather_slot(pr, (tile + stride) * 128u + t, n, nxt);
+    } else if (row < n) {
+      r0 = rec[3 * (size_t)row];
+      r1 = rec[3 * (size_t)row + 1];
+      r2 = rec[3 * (size_t)row + 2];
+    }
     write_features(A, t, r0, r1, r2, p);
     bool ok = true;
     for (int l = 0; l < 4 && ok; ++l) {
@@ -285,6 +314,7 @@ __global__ void __launch_bounds__(kInferTPB) k_mlp_infer(const float4 *__restric
       if (ok && l < 3) epilogue_relu(lane_addr, A, t);
     }
     if (!ok) break;
+    if (PATHS) gather_hit(pr, nxt);
     float e[64];
     const bool full = p.nclusters == 64;
     const float sum = full ? softmax_exp64(lane_addr, e) : softmax_exp(lane_addr, p.nclusters, e);
@@ -333,6 +363,7 @@ __global__ void __launch_bounds__(kInferTPB) k_mlp_infer(const float4 *__restric
                             *reinterpret_cast<uint32_t *>(&h2), *reinterpret_cast<uint32_t *>(&h3));
       }
     }
+    if (PATHS) cur = nxt;
     tc::fence_before_sync();
     group_sync(g);
   }

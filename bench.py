@@ -348,17 +348,18 @@ def bench_manylight(torch):
                          "lr": opts["lr"]}}
 
 
-def bench_batch(torch):
-    """64 box-scene jobs (random sphere BRDFs GGX/Beckmann/Phong with roughness in
-    [0.05, 0.9], camera yaw in [-30, 30] degrees, resolution from {256..1024}^2, spp
-    from {4, 16, 64}, depth from {3, 6}), path tracer with MIS: one wavefront pass
+def bench_batch(torch, njobs=64, sizes=(256, 512, 768, 1024), spps=(4, 16, 64)):
+    """Box-scene jobs (random sphere BRDFs GGX/Beckmann/Phong with roughness in
+    [0.05, 0.9], camera yaw in [-30, 30] degrees, square resolution from `sizes`, spp
+    from `spps`, depth from {3, 6}), path tracer with MIS: one wavefront pass
     replayed from a CUDA graph (block and wave sizes from the autotuner) against the
-    same jobs rendered one after another with their own launches."""
+    same jobs rendered one after another with their own launches, and against one
+    ckr_render call per job."""
     from chakumrender_gb300 import scene as S
     from chakumrender_gb300.batch import Batch, Job, box_jobs
 
     sd = S.load_xml(S.SCENES / "box.xml")
-    params, mats = box_jobs(sd, njobs=64, seed=4)
+    params, mats = box_jobs(sd, njobs=njobs, seed=4, sizes=sizes, spps=spps)
     outs = [torch.empty((p["cam"].height, p["cam"].width, 3), dtype=torch.float32, device="cuda") for p in params]
     jobs = [Job(p["cam"], p["spp"], p["max_depth"], p["seed"], p["material_set"], 0, o.data_ptr())
             for p, o in zip(params, outs)]
@@ -394,8 +395,8 @@ def bench_batch(torch):
         ev[3].record(s)
         torch.cuda.synchronize()
     t_api = ev[2].elapsed_time(ev[3]) / 1e3
-    return {"workload": "64 box-scene jobs, random sphere BRDFs and yaw, 256^2..1024^2, 4/16/64 spp, depth 3/6, "
-                        "path tracer with MIS",
+    return {"workload": (f"{njobs} box-scene jobs, random sphere BRDFs and yaw, {min(sizes)}^2..{max(sizes)}^2, "
+                         f"{'/'.join(map(str, spps))} spp, depth 3/6, path tracer with MIS"),
             "samples": paths, "graph_launches": launches,
             "batched_graph": {"sec": round(t_graph, 4), "samples_per_s": round(paths / t_graph, 1)},
             "sequential_per_job": {"sec": round(t_seq, 4), "samples_per_s": round(paths / t_seq, 1)},
@@ -647,6 +648,8 @@ def main():
     line["ltc_shade"] = bench_ltc(torch, args.steps)
     line["manylight"] = bench_manylight(torch)
     line["batch"] = bench_batch(torch)
+    # Many small jobs: launch-bound when each is rendered on its own.
+    line["batch_small"] = bench_batch(torch, njobs=512, sizes=(32, 48, 64), spps=(1, 2, 4))
     if not args.no_cpu_baseline:
         cb, ref_counts = cpu_baseline(tri, closest)
         line["cpu_baseline"] = cb

@@ -76,10 +76,23 @@ __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// A bounded wait gives up after this long whatever its poll count: one try_wait may
+// suspend the thread for an implementation-defined time, so a count alone does not
+// bound the wait in time.
+constexpr uint64_t kMbarWaitNs = 1000000000ull;  // 1 s; an MMA chain takes microseconds
+
 // Waits for the phase with parity `parity` to complete; gives up after `tries`
-// polls (returns false) so that a lost arrival cannot hang the GPU.
+// polls or kMbarWaitNs (returns false) so that a lost arrival cannot hang the GPU.
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint32_t tries) {
+  const uint64_t t0 = globaltimer_ns();
   for (uint32_t i = 0; i < tries; ++i) {
+    if ((i & 255u) == 255u && globaltimer_ns() - t0 > kMbarWaitNs) return false;
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"

@@ -261,9 +261,13 @@ int trace_host(ckr_scene *s, const ckr_ray *rays, uint32_t n, uint32_t *hit_id, 
   // Order after prior work on the caller's stream.
   CKR_CUDA_TRY(cudaEventRecord(s->user_ready, user));
   for (int k = 0; k < kPipes; ++k) CKR_CUDA_TRY(cudaStreamWaitEvent(s->pipe[k], s->user_ready, 0));
-  uint32_t k = 0;
-  for (uint32_t off = 0; off < n; off += chunk, ++k) {
-    uint32_t m = std::min(chunk, n - off);
+  // Chunks grow from kHostChunk / 8 to kHostChunk, so that the first upload, which
+  // nothing overlaps, is short (e2e 3088 -> 3118 Mrays/s; shrinking the last chunks
+  // as well was slower, 3035).
+  uint32_t k = 0, size = chunk >> 3;
+  for (uint32_t off = 0; off < n; ++k) {
+    const uint32_t m = std::min(size, n - off);
+    size = std::min(size * 2, chunk);
     int slot = (int)(k % kPipes);
     cudaStream_t st = s->pipe[slot];
     size_t base = (size_t)slot * chunk;
@@ -280,7 +284,7 @@ int trace_host(ckr_scene *s, const ckr_ray *rays, uint32_t n, uint32_t *hit_id, 
       CKR_CUDA_TRY(cudaMemcpyAsync(hit_id + off, s->st_id.ptr + base, (size_t)m * 4, cudaMemcpyDeviceToHost, st));
       CKR_CUDA_TRY(cudaMemcpyAsync(hit_t + off, s->st_t.ptr + base, (size_t)m * 4, cudaMemcpyDeviceToHost, st));
     }
-    if (n - off <= chunk) break;
+    off += m;
   }
   for (int k = 0; k < kPipes; ++k) {
     CKR_CUDA_TRY(cudaEventRecord(s->pipe_done[k], s->pipe[k]));

@@ -1,10 +1,12 @@
 // trace.cu — scene upload and the closest-hit / any-hit traversal kernels.
 //
-// One thread per ray; a persistent grid (a multiple of the SM count) strides
-// over the ray list.  Each thread keeps its traversal stack in shared memory,
-// laid out level-major ([level][thread]) so stack traffic is bank-conflict
-// free.  BVH nodes (64 B: both child boxes + links) and triangles (48 B) are
-// read with 16-byte read-only loads.
+// A persistent grid (the SMs x the blocks that fit) fetches rays dynamically
+// (trace_dynamic): a lane takes a new ray when its own is finished.  Each lane
+// keeps its traversal stack of node groups in shared memory, laid out level-major
+// ([level][thread]) so stack traffic is bank-conflict free.  Wide nodes (80 B:
+// eight quantised child boxes) and triangles (48 B) are read with 16-byte
+// read-only loads.  The host-buffer entry points pipeline uploads, traversal and
+// downloads over internal streams.
 #include <algorithm>
 #include <chrono>
 #include <cstring>

@@ -177,7 +177,7 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
                          : cfg->shader == CKR_SHADER_PATH      ? (const void *)k_shade_path<kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_CV  ? (const void *)k_shade<CKR_SHADER_DIRECT_CV, kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_MIS ? (const void *)k_shade<CKR_SHADER_DIRECT_MIS, kRTPB>
-                                                                : (const void *)k_shade<CKR_SHADER_DIRECT_MISCV, kRTPB>;
+                                                                : (const void *)k_shade_miscv<kRTPB>;
   const int g_shade = grid_for(shade_fn, cfg->shader == CKR_SHADER_EXPLICIT ? smem : 0, kRTPB);
   for (uint64_t base = 0; base < total; base += wave) {
     uint32_t n = (uint32_t)std::min<uint64_t>(wave, total - base);
@@ -222,7 +222,7 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
       else if (cfg->shader == CKR_SHADER_DIRECT_MIS)
         k_shade<CKR_SHADER_DIRECT_MIS, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else
-        k_shade<CKR_SHADER_DIRECT_MISCV, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
+        k_shade_miscv<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       shadow_fn<<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur, train ? prop->rec.ptr : nullptr);
       if (train) {
         // Adam steps on this bounce's light samples (visibility applied above),
@@ -435,7 +435,7 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
                          : cfg->shader == CKR_SHADER_PATH      ? (const void *)k_shade_path<kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_CV  ? (const void *)k_shade<CKR_SHADER_DIRECT_CV, kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_MIS ? (const void *)k_shade<CKR_SHADER_DIRECT_MIS, kRTPB>
-                                                                : (const void *)k_shade<CKR_SHADER_DIRECT_MISCV, kRTPB>;
+                                                                : (const void *)k_shade_miscv<kRTPB>;
   const int g_shade = grid_for(shade_fn, 0, kRTPB);
   for (uint64_t base = 0; base < total; base += wave) {
     uint32_t n = (uint32_t)std::min<uint64_t>(wave, total - base);
@@ -456,7 +456,7 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
       else if (cfg->shader == CKR_SHADER_DIRECT_MIS)
         k_shade<CKR_SHADER_DIRECT_MIS, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else
-        k_shade<CKR_SHADER_DIRECT_MISCV, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
+        k_shade_miscv<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       shadow_fn<<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur, nullptr);
       cur ^= 1;
       if (!path) break;

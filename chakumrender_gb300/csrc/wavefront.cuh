@@ -649,8 +649,7 @@ __device__ __forceinline__ void shade(ShadeView sv0, Paths P, Params prm, int cu
 // Shading kernels.  The MIS path tracer's vertex is register hungry but short: at
 // 640 / TPB resident blocks (96 registers at 128 threads, with some spills) the box
 // frame took 1.50 ms against 1.65 ms at the default 149 registers.  The direct-light
-// shaders keep the compiler's choice (the MISCV shader at 188 spill-free registers was
-// 38 % slower than at its default 128).
+// shaders keep the compiler's choice, except MISCV (k_shade_miscv below).
 template <uint32_t SHADER, int TPB>
 __global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params prm, int cur, int depth,
                                                  const LtcEntry *__restrict__ ltc, SceneView scene = SceneView{},
@@ -662,6 +661,14 @@ template <int TPB>
 __global__ void __launch_bounds__(TPB, (640 / TPB > 1 ? 640 / TPB : 1))
     k_shade_path(ShadeView sv0, Paths P, Params prm, int cur, int depth, const LtcEntry *__restrict__ ltc) {
   shade<CKR_SHADER_PATH, TPB>(sv0, P, prm, cur, depth, ltc, SceneView{}, 0);
+}
+
+// The reference's default shader (MISCV) at 512 / TPB resident blocks (128
+// registers at 128 threads): at 154 spill-free registers it was 8 % slower.
+template <int TPB>
+__global__ void __launch_bounds__(TPB, (512 / TPB > 1 ? 512 / TPB : 1))
+    k_shade_miscv(ShadeView sv0, Paths P, Params prm, int cur, int depth, const LtcEntry *__restrict__ ltc) {
+  shade<CKR_SHADER_DIRECT_MISCV, TPB>(sv0, P, prm, cur, depth, ltc, SceneView{}, 0);
 }
 
 // CKR_SHADER_PATH_NEE: one light sample and one BRDF sample per vertex over many

@@ -501,7 +501,27 @@ def case_trace():
         raise SystemExit("device status error")
 
 
-CASES = {"manylight-learned": case_manylight_learned, "manylight-split": case_manylight_split, "trace": case_trace}
+def case_ltc():
+    """LTC shading of the 1024x1024 G-buffer with 8 quad lights, three launches, for
+    profilers."""
+    import torch
+    from chakumrender_gb300 import build
+    from chakumrender_gb300 import ckr
+
+    build.build_library()
+    n = 1024 * 1024
+    g = torch.from_numpy(ckr.gbuffer(2, n)).cuda()
+    lt, lc = ckr.quad_lights(3, 8)
+    dt, dc = torch.from_numpy(lt).cuda(), torch.from_numpy(lc).cuda()
+    out = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    for _ in range(3):
+        ckr.ltc_shade(g.data_ptr(), n, dt.data_ptr(), dc.data_ptr(), len(lt), out.data_ptr(), s)
+    torch.cuda.synchronize()
+
+
+CASES = {"manylight-learned": case_manylight_learned, "manylight-split": case_manylight_split, "trace": case_trace,
+         "ltc": case_ltc}
 
 
 def main():

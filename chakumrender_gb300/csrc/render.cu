@@ -190,7 +190,11 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
       CKR_CUDA_TRY(cudaMemsetAsync(P.counts + (cur ^ 1), 0, sizeof(uint32_t), stream));
       CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), stream));
       Learn lr{};
-      if (prop) {
+      // Vertices at the last depth only add emission: no light sample, so neither
+      // a light distribution nor training records there.
+      const bool nee = d < prm.max_depth;
+      if (prop) lr.sel_prev = d ? prop->sel[(d - 1) & 1].ptr : nullptr;
+      if (prop && nee) {
         // Light distributions at this bounce's vertices.
         mlp::PathRows pr;
         pr.queue = cur ? P.q1 : P.q0;
@@ -204,7 +208,6 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
                                   prop->defensive, stream);
         if (ms != CKR_OK) return ms;
         lr.sel = prop->sel[d & 1].ptr;
-        lr.sel_prev = d ? prop->sel[(d - 1) & 1].ptr : nullptr;
         if (train) {
           lr.rec = prop->rec.ptr;
           lr.rec_count = prop->rec_count.ptr;
@@ -223,8 +226,8 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
         k_shade<CKR_SHADER_DIRECT_MIS, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else
         k_shade_miscv<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
-      shadow_fn<<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur, train ? prop->rec.ptr : nullptr);
-      if (train) {
+      shadow_fn<<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur, train && nee ? prop->rec.ptr : nullptr);
+      if (train && nee) {
         // Adam steps on this bounce's light samples (visibility applied above),
         // minibatch by minibatch; steps past the records actually written are no-ops.
         for (uint32_t off = 0; off < prop->batch; off += prop->minibatch) {

@@ -113,8 +113,10 @@ int ckr_trace_any(const ckr_scene *scene, const ckr_ray *rays, uint32_t n,
 
 /* Host-buffer forms of the two queries (the drop-in for callers that hold
  * rays in host memory, as every reference caller does): copy rays in, trace,
- * copy results out, in chunks that overlap copies with traversal.  Staging
- * buffers are owned by the scene and reused. */
+ * copy results out, in chunks that overlap copies with traversal.  Rays in
+ * pinned memory whose address is 16-byte aligned are read in place by the
+ * kernels instead of being copied in.  Staging buffers are owned by the scene
+ * and reused. */
 int ckr_trace_closest_host(ckr_scene *scene, const ckr_ray *rays, uint32_t n,
                            uint32_t *hit_id, float *hit_t, void *stream);
 int ckr_trace_any_host(ckr_scene *scene, const ckr_ray *rays, uint32_t n,

@@ -10,7 +10,8 @@
 // costs C_trav = 1 and C_isect = 1 per triangle; large subtrees are built on
 // separate threads.  The binary tree is then collapsed into eight-wide nodes
 // with 8-bit quantised child boxes (Ylitie, Karras, Laine, HPG 2017; layout in
-// bvh_build.h).
+// bvh_build.h); the collapse's plan and the writing of the wide nodes run on
+// several threads too, with the same output as a single thread.
 #include "bvh_build.h"
 
 #include <algorithm>
@@ -18,6 +19,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <memory>
 #include <thread>
 
 namespace ckr {
@@ -61,6 +63,7 @@ struct TNode {
   uint32_t left;   // index of left child in the node pool (right = left + 1)
   uint32_t begin;  // leaf: first prim index
   uint32_t count;  // leaf: prim count; 0 for interior
+  uint32_t size;   // prims in the subtree
 };
 
 struct Builder {
@@ -82,6 +85,7 @@ struct Builder {
   void build(uint32_t ni, uint32_t begin, uint32_t end) {
     TNode &node = pool[ni];
     uint32_t n = end - begin;
+    node.size = n;
     if (n <= 1) {
       make_leaf(node, begin, end);
       return;
@@ -198,172 +202,280 @@ struct Entry {
 // equal.
 constexpr float kCostNode = 1.0f, kCostPrim = 1.0f;
 
+// Subtrees of at least this many triangles are handed to another thread while
+// spare threads remain (plan and emission alike).
+constexpr uint32_t kParallelPrims = 1u << 15;
+
 // Optimal collapse of the binary tree (the dynamic programme of Ylitie et al.
 // 2017).  For binary node n, cost[8n + j - 1] is the least cost of spreading n's
 // subtree over at most j slots of the wide node above it: n itself in one slot
 // (as a leaf of <= leaf_max triangles or as a wide node of its own), or the
-// slots shared between its two children.
+// slots shared between its two children.  wide[8n + j - 1] counts the wide nodes
+// that choice creates, so that every wide subtree's place in the output is known
+// before it is written.
 struct Plan {
-  std::vector<float> cost;
-  std::vector<uint8_t> split;   // per (n, j): 0 = n takes one slot, k = k slots to the left child
-  std::vector<uint8_t> leaf;    // n in one slot is a leaf (else a wide node)
-  std::vector<uint8_t> wsplit;  // n as a wide node: slots of its left child (right: 8 - wsplit)
-  std::vector<uint32_t> begin, count;  // n's triangles: prims[begin, begin + count)
+  // Every entry of a binary node is written when the node is planned, so the
+  // arrays are left uninitialised (a few hundred MB at a million triangles).
+  std::unique_ptr<float[]> cost;
+  std::unique_ptr<uint32_t[]> wide;
+  std::unique_ptr<uint8_t[]> split;   // per (n, j): 0 = n takes one slot, k = k slots to the left child
+  std::unique_ptr<uint8_t[]> leaf;    // n in one slot is a leaf (else a wide node)
+  std::unique_ptr<uint8_t[]> wsplit;  // n as a wide node: slots of its left child (right: 8 - wsplit)
+  std::unique_ptr<uint32_t[]> begin, count;  // n's triangles: prims[begin, begin + count)
+
+  explicit Plan(uint32_t N)
+      : cost(new float[(size_t)N * 8]), wide(new uint32_t[(size_t)N * 8]), split(new uint8_t[(size_t)N * 8]),
+        leaf(new uint8_t[N]), wsplit(new uint8_t[N]), begin(new uint32_t[N]), count(new uint32_t[N]) {}
+
+  // Wide nodes below interior binary node n made a wide node (its descendants).
+  uint32_t below(const Builder &b, uint32_t n) const {
+    const uint32_t L = b.pool[n].left;
+    return wide[(size_t)L * 8 + wsplit[n] - 1] + wide[(size_t)(L + 1) * 8 + (8 - wsplit[n]) - 1];
+  }
 };
 
-void make_plan(const Builder &b, uint32_t leaf_max, Plan &p) {
-  const uint32_t N = b.next.load();
-  p.cost.assign((size_t)N * 8, 0.f);
-  p.split.assign((size_t)N * 8, 0);
-  p.leaf.assign(N, 0);
-  p.wsplit.assign(N, 1);
-  p.begin.assign(N, 0);
-  p.count.assign(N, 0);
-  // Children are allocated after their parent: reverse index order is bottom-up.
-  for (uint32_t i = N; i-- > 0;) {
-    const TNode &n = b.pool[i];
-    float *d = &p.cost[(size_t)i * 8];
-    const float area = n.box.area();
-    if (n.count) {  // binary leaf (one triangle: the binary tree is built with leaf size 1)
-      p.begin[i] = n.begin;
-      p.count[i] = n.count;
-      p.leaf[i] = 1;
-      for (int j = 0; j < 8; ++j) d[j] = area * (float)n.count * kCostPrim;
-      continue;
+// The plan's entries of binary node i from those of its children.
+void plan_node(const Builder &b, uint32_t leaf_max, Plan &p, uint32_t i) {
+  const TNode &n = b.pool[i];
+  float *d = &p.cost[(size_t)i * 8];
+  uint32_t *w = &p.wide[(size_t)i * 8];
+  const float area = n.box.area();
+  uint8_t *sp = &p.split[(size_t)i * 8];
+  if (n.count) {  // binary leaf (one triangle: the binary tree is built with leaf size 1)
+    p.begin[i] = n.begin;
+    p.count[i] = n.count;
+    p.leaf[i] = 1;
+    p.wsplit[i] = 1;
+    for (int j = 0; j < 8; ++j) {
+      d[j] = area * (float)n.count * kCostPrim;
+      w[j] = 0;
+      sp[j] = 0;
     }
-    const uint32_t L = n.left, R = L + 1;
-    p.begin[i] = p.begin[L];
-    p.count[i] = p.count[L] + p.count[R];
-    const float *dl = &p.cost[(size_t)L * 8], *dr = &p.cost[(size_t)R * 8];
-    float best = std::numeric_limits<float>::infinity();
-    int bk = 1;
-    for (int k = 1; k <= 7; ++k) {
-      const float c = dl[k - 1] + dr[8 - k - 1];
-      if (c < best) {
-        best = c;
-        bk = k;
+    return;
+  }
+  const uint32_t L = n.left, R = L + 1;
+  p.begin[i] = p.begin[L];
+  p.count[i] = p.count[L] + p.count[R];
+  const float *dl = &p.cost[(size_t)L * 8], *dr = &p.cost[(size_t)R * 8];
+  const uint32_t *wl = &p.wide[(size_t)L * 8], *wr = &p.wide[(size_t)R * 8];
+  float best = std::numeric_limits<float>::infinity();
+  int bk = 1;
+  for (int k = 1; k <= 7; ++k) {
+    const float c = dl[k - 1] + dr[8 - k - 1];
+    if (c < best) {
+      best = c;
+      bk = k;
+    }
+  }
+  const float c_wide = area * kCostNode + best;
+  const float c_leaf = p.count[i] <= leaf_max ? area * (float)p.count[i] * kCostPrim
+                                              : std::numeric_limits<float>::infinity();
+  const float c1 = std::min(c_leaf, c_wide);
+  p.leaf[i] = c_leaf <= c_wide;
+  p.wsplit[i] = (uint8_t)bk;
+  d[0] = c1;
+  w[0] = p.leaf[i] ? 0u : 1u + wl[bk - 1] + wr[8 - bk - 1];
+  sp[0] = 0;
+  for (int j = 2; j <= 8; ++j) {
+    float bj = c1;
+    int sj = 0;
+    for (int k = 1; k < j; ++k) {
+      const float c = dl[k - 1] + dr[j - k - 1];
+      if (c < bj) {
+        bj = c;
+        sj = k;
       }
     }
-    const float c_wide = area * kCostNode + best;
-    const float c_leaf = p.count[i] <= leaf_max ? area * (float)p.count[i] * kCostPrim
-                                                : std::numeric_limits<float>::infinity();
-    const float c1 = std::min(c_leaf, c_wide);
-    p.leaf[i] = c_leaf <= c_wide;
-    p.wsplit[i] = (uint8_t)bk;
-    d[0] = c1;
-    for (int j = 2; j <= 8; ++j) {
-      float bj = c1;
-      int sj = 0;
-      for (int k = 1; k < j; ++k) {
-        const float c = dl[k - 1] + dr[j - k - 1];
-        if (c < bj) {
-          bj = c;
-          sj = k;
-        }
-      }
-      d[j - 1] = bj;
-      p.split[(size_t)i * 8 + j - 1] = (uint8_t)sj;
-    }
+    d[j - 1] = bj;
+    w[j - 1] = sj ? wl[sj - 1] + wr[j - sj - 1] : w[0];
+    sp[j - 1] = (uint8_t)sj;
   }
 }
 
-// The slot children of binary node n spread over at most j slots.
-void gather(const Builder &b, const Plan &p, uint32_t n, uint32_t j, std::vector<Entry> &out) {
+// Plans the subtree of binary node `root`, children before parents.  While spare
+// threads remain, a large subtree's left half goes to another thread (joined
+// before the node itself is planned); the rest is an explicit-stack post-order.
+void plan_subtree(const Builder &b, uint32_t leaf_max, Plan &p, uint32_t root, std::atomic<int> &spare) {
+  const TNode &r = b.pool[root];
+  if (r.count == 0 && r.size >= kParallelPrims && spare.fetch_sub(1) > 0) {
+    std::thread t([&b, leaf_max, &p, &r, &spare] { plan_subtree(b, leaf_max, p, r.left, spare); });
+    plan_subtree(b, leaf_max, p, r.left + 1, spare);
+    t.join();
+    spare.fetch_add(1);
+    plan_node(b, leaf_max, p, root);
+    return;
+  }
+  if (r.count == 0 && r.size >= kParallelPrims) spare.fetch_add(1);
+  struct Item {
+    uint32_t node;
+    bool expanded;
+  };
+  std::vector<Item> stack{{root, false}};
+  while (!stack.empty()) {
+    const Item it = stack.back();
+    stack.pop_back();
+    const TNode &n = b.pool[it.node];
+    if (it.expanded || n.count) {
+      plan_node(b, leaf_max, p, it.node);
+      continue;
+    }
+    stack.push_back({it.node, true});
+    stack.push_back({n.left + 1, false});
+    stack.push_back({n.left, false});
+  }
+}
+
+// The slot children of binary node n spread over at most j slots, appended to
+// kids[0 .. nk).
+void gather(const Builder &b, const Plan &p, uint32_t n, uint32_t j, Entry *kids, int &nk) {
   const uint32_t s = p.split[(size_t)n * 8 + j - 1];
   if (s == 0) {
     if (p.leaf[n])
-      out.push_back({b.pool[n].box, 0, p.begin[n], p.count[n]});
+      kids[nk++] = {b.pool[n].box, 0, p.begin[n], p.count[n]};
     else
-      out.push_back({b.pool[n].box, n, 0, 0});
+      kids[nk++] = {b.pool[n].box, n, 0, 0};
     return;
   }
-  gather(b, p, b.pool[n].left, s, out);
-  gather(b, p, b.pool[n].left + 1, j - s, out);
+  gather(b, p, b.pool[n].left, s, kids, nk);
+  gather(b, p, b.pool[n].left + 1, j - s, kids, nk);
 }
 
-// Collapses the binary tree into wide nodes following the plan.  Children go to
-// slots by a greedy assignment on cost(child, slot) = (centroid - node centre) .
-// dir(slot), dir = the octant's signs, so that slot o holds the child nearest the
-// start of rays travelling in octant o.  Boxes are quantised outward.
-void collapse(const Builder &b, const float *tri9, uint32_t leaf_max, FlatBvh &out) {
-  const uint32_t n = (uint32_t)b.prims.size();
-  Plan plan;
-  make_plan(b, leaf_max, plan);
-  out.tris.reserve((size_t)n * 12);
-  out.nnodes_binary = 0;
-  for (uint32_t i = 0; i < (uint32_t)b.next.load(); ++i)
-    if (b.pool[i].count == 0) out.nnodes_binary++;
+// Float to an unsigned key with the same order (no NaN); -0 is taken as +0.
+inline uint32_t order_key(float f) {
+  uint32_t u;
+  f += 0.0f;
+  std::memcpy(&u, &f, 4);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// Writes the wide tree into out.nodes / out.tris.  The output order is the one a
+// depth-first emission gives: a node's interior children get consecutive indices
+// when the node is written, the first slot's subtree is written next, and a node's
+// leaf triangles are appended when it is written.  With the plan's wide-node counts
+// every subtree's first node index, first child index and first triangle are known
+// up front, so subtrees are written by several threads into disjoint ranges.
+struct Emitter {
+  const Builder &b;
+  const Plan &p;
+  const float *tri9;
+  FlatBvh &out;
+  std::atomic<int> &spare;
+  std::atomic<uint32_t> nleaves{0}, max_depth{0};
+
   struct Work {
-    uint32_t tnode, index, depth;
+    uint32_t tnode, index, child_base, tri_base, depth;
   };
-  std::vector<Work> work{{0, 0, 1}};
-  out.nnodes = 1;
-  out.root = 0;
-  std::vector<Entry> kids;
-  while (!work.empty()) {
-    Work wk = work.back();
-    work.pop_back();
-    out.max_depth = std::max(out.max_depth, wk.depth);
-    const TNode &tn = b.pool[wk.tnode];
-    kids.clear();
-    if (tn.count > 0) {
-      kids.push_back({tn.box, 0, tn.begin, tn.count});  // the whole tree is one triangle
-    } else {
-      gather(b, plan, tn.left, plan.wsplit[wk.tnode], kids);
-      gather(b, plan, tn.left + 1, 8 - plan.wsplit[wk.tnode], kids);
+
+  // Writes the subtree of `root` (a wide node) and everything below it.
+  void run(Work root) {
+    std::vector<Work> work{root};
+    std::vector<std::thread> threads;
+    uint32_t leaves = 0, depth_max = 0;
+    while (!work.empty()) {
+      const Work wk = work.back();
+      work.pop_back();
+      depth_max = std::max(depth_max, wk.depth);
+      Entry kids[8];
+      int nk = 0;
+      const TNode &tn = b.pool[wk.tnode];
+      if (tn.count > 0) {
+        kids[nk++] = {tn.box, 0, tn.begin, tn.count};  // the whole tree is one triangle
+      } else {
+        gather(b, p, tn.left, p.wsplit[wk.tnode], kids, nk);
+        gather(b, p, tn.left + 1, 8 - p.wsplit[wk.tnode], kids, nk);
+      }
+      int slot_kid[8];
+      uint32_t nint = 0, ntri = 0;
+      write_node(wk, kids, nk, slot_kid, nint, ntri, leaves);
+      // Children in slot order: indices child_base + k, their own children and
+      // triangles after everything written before them.
+      uint32_t cb = wk.child_base + nint, tb = wk.tri_base + ntri, k = 0;
+      Work child[8];
+      for (int slot = 0; slot < 8; ++slot) {
+        if (slot_kid[slot] < 0 || kids[slot_kid[slot]].count != 0) continue;
+        const uint32_t c = kids[slot_kid[slot]].tnode;
+        child[k] = {c, wk.child_base + k, cb, tb, wk.depth + 1};
+        cb += p.below(b, c);
+        tb += p.count[c];
+        ++k;
+      }
+      for (uint32_t i = k; i-- > 0;) {
+        if (b.pool[child[i].tnode].size >= kParallelPrims && spare.fetch_sub(1) > 0) {
+          threads.emplace_back([this, w = child[i]] {
+            run(w);
+            spare.fetch_add(1);
+          });
+          continue;
+        }
+        if (b.pool[child[i].tnode].size >= kParallelPrims) spare.fetch_add(1);
+        work.push_back(child[i]);
+      }
     }
+    for (std::thread &t : threads) t.join();
+    nleaves.fetch_add(leaves);
+    uint32_t m = max_depth.load();
+    while (m < depth_max && !max_depth.compare_exchange_weak(m, depth_max)) {
+    }
+  }
+
+  // One wide node: slot assignment, quantised boxes, meta bytes, its leaf
+  // children's triangles.  Out: slot -> kid (-1: empty), interior children and
+  // triangles written.
+  void write_node(const Work &wk, const Entry *kids, int nk, int *slot_kid, uint32_t &nint, uint32_t &ntri,
+                  uint32_t &leaves) {
     // Node box and quantisation grid.
     Box nb;
     nb.reset();
-    for (const Entry &e : kids) nb.grow(e.box);
+    for (int k = 0; k < nk; ++k) nb.grow(kids[k].box);
     float centre[3];
     for (int a = 0; a < 3; ++a) centre[a] = 0.5f * nb.lo[a] + 0.5f * nb.hi[a];
-    // Greedy slot assignment over all (child, slot) pairs, cheapest first.
-    struct Pair {
-      float cost;
-      int kid, slot;
-    };
-    Pair pairs[64];
+    // Children go to slots by a greedy assignment on cost(child, slot) = (centroid
+    // - node centre) . dir(slot), dir = the octant's signs, cheapest pair first
+    // (ties: lower child, then lower slot), so that slot o holds the child nearest
+    // the start of rays travelling in octant o.
+    uint64_t keys[64];
     int np = 0;
-    for (int k = 0; k < (int)kids.size(); ++k) {
+    for (int k = 0; k < nk; ++k) {
       float c[3];
       for (int a = 0; a < 3; ++a) c[a] = 0.5f * kids[k].box.lo[a] + 0.5f * kids[k].box.hi[a] - centre[a];
       for (int slot = 0; slot < 8; ++slot) {
-        float cost = ((slot & 4) ? -c[0] : c[0]) + ((slot & 2) ? -c[1] : c[1]) + ((slot & 1) ? -c[2] : c[2]);
-        pairs[np++] = {cost, k, slot};
+        const float cost = ((slot & 4) ? -c[0] : c[0]) + ((slot & 2) ? -c[1] : c[1]) + ((slot & 1) ? -c[2] : c[2]);
+        keys[np++] = (uint64_t)order_key(cost) << 32 | (uint32_t)(k * 8 + slot);
       }
     }
-    std::stable_sort(pairs, pairs + np, [](const Pair &x, const Pair &y) { return x.cost < y.cost; });
-    int slot_kid[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+    std::sort(keys, keys + np);
     bool placed[8] = {false, false, false, false, false, false, false, false};
-    for (int i = 0; i < np; ++i)
-      if (slot_kid[pairs[i].slot] < 0 && !placed[pairs[i].kid]) {
-        slot_kid[pairs[i].slot] = pairs[i].kid;
-        placed[pairs[i].kid] = true;
+    for (int s = 0; s < 8; ++s) slot_kid[s] = -1;
+    for (int i = 0; i < np; ++i) {
+      const int kid = (int)((keys[i] & 0xffffffffu) >> 3), slot = (int)(keys[i] & 7u);
+      if (slot_kid[slot] < 0 && !placed[kid]) {
+        slot_kid[slot] = kid;
+        placed[kid] = true;
       }
+    }
     uint32_t w[kWideWords] = {};
     std::memcpy(&w[0], &nb.lo[0], 12);
     int e[3];
     for (int a = 0; a < 3; ++a) {
-      const double p = nb.lo[a], hi = nb.hi[a], ext = hi - p;
+      const double p0 = nb.lo[a], hi = nb.hi[a], ext = hi - p0;
       int ex = -126;
       if (ext > 0.0) {
         std::frexp(ext / 255.0, &ex);  // 2^ex > ext / 255
-        while (ex > -126 && p + 255.0 * std::ldexp(1.0, ex - 1) >= hi) --ex;
-        while (p + 255.0 * std::ldexp(1.0, ex) < hi) ++ex;
+        while (ex > -126 && p0 + 255.0 * std::ldexp(1.0, ex - 1) >= hi) --ex;
+        while (p0 + 255.0 * std::ldexp(1.0, ex) < hi) ++ex;
       }
       e[a] = std::max(-126, std::min(127, ex));
       w[3] |= (uint32_t)(e[a] + 127) << (8 * a);
     }
     uint8_t meta[8] = {}, q[6][8] = {};
-    uint32_t imask = 0, nint = 0;
-    const uint32_t child_base = out.nnodes, tri_base = (uint32_t)(out.tris.size() / 12);
+    uint32_t imask = 0;
+    nint = ntri = 0;
     for (int slot = 0; slot < 8; ++slot) {
       if (slot_kid[slot] < 0) continue;
       const Entry &c = kids[slot_kid[slot]];
       for (int a = 0; a < 3; ++a) {
-        const double p = nb.lo[a], step = std::ldexp(1.0, e[a]);
-        double lo = std::floor(((double)c.box.lo[a] - p) / step), hi = std::ceil(((double)c.box.hi[a] - p) / step);
+        const double p0 = nb.lo[a], step = std::ldexp(1.0, e[a]);
+        double lo = std::floor(((double)c.box.lo[a] - p0) / step), hi = std::ceil(((double)c.box.hi[a] - p0) / step);
         uint32_t ql = (uint32_t)std::max(0.0, std::min(255.0, lo)), qh = (uint32_t)std::max(0.0, std::min(255.0, hi));
         while (ql > 0 && plane(nb.lo[a], ql, e[a]) > (double)c.box.lo[a]) --ql;
         while (qh < 255 && plane(nb.lo[a], qh, e[a]) < (double)c.box.hi[a]) ++qh;
@@ -375,32 +487,43 @@ void collapse(const Builder &b, const float *tri9, uint32_t leaf_max, FlatBvh &o
         meta[slot] = (uint8_t)(0x38 + slot);
         ++nint;
       } else {
-        const uint32_t off = (uint32_t)(out.tris.size() / 12) - tri_base;
-        meta[slot] = (uint8_t)((((1u << c.count) - 1u) << 5) | off);
+        meta[slot] = (uint8_t)((((1u << c.count) - 1u) << 5) | ntri);
         for (uint32_t i = c.begin; i < c.begin + c.count; ++i) {
           const float *t = tri9 + 9 * (size_t)b.prims[i].id;
-          float rec[12] = {t[0], t[1], t[2], 0.f, t[3], t[4], t[5], 0.f, t[6], t[7], t[8], 0.f};
+          float *rec = &out.tris[(size_t)(wk.tri_base + ntri++) * 12];
+          const float r[12] = {t[0], t[1], t[2], 0.f, t[3], t[4], t[5], 0.f, t[6], t[7], t[8], 0.f};
+          std::memcpy(rec, r, sizeof(r));
           std::memcpy(&rec[3], &b.prims[i].id, 4);
-          out.tris.insert(out.tris.end(), rec, rec + 12);
         }
-        out.nleaves++;
+        ++leaves;
       }
     }
     w[3] |= imask << 24;
-    w[4] = child_base;
-    w[5] = tri_base;
+    w[4] = wk.child_base;
+    w[5] = wk.tri_base;
     std::memcpy(&w[6], meta, 8);
     std::memcpy(&w[8], q, 48);
-    if (out.nodes.size() < (size_t)(wk.index + 1) * kWideWords) out.nodes.resize((size_t)(wk.index + 1) * kWideWords);
     std::memcpy(&out.nodes[(size_t)wk.index * kWideWords], w, sizeof(w));
-    // Interior children get consecutive indices in slot order; the first slot's
-    // subtree is processed next (depth first).
-    out.nnodes += nint;
-    uint32_t k = nint;
-    for (int slot = 7; slot >= 0; --slot)
-      if ((imask >> slot) & 1u) work.push_back({kids[slot_kid[slot]].tnode, child_base + --k, wk.depth + 1});
   }
-  out.nodes.resize((size_t)out.nnodes * kWideWords);
+};
+
+void collapse(const Builder &b, const float *tri9, uint32_t leaf_max, uint32_t threads, FlatBvh &out) {
+  const uint32_t n = (uint32_t)b.prims.size();
+  const uint32_t N = b.next.load();
+  Plan plan(N);
+  std::atomic<int> spare{(int)threads - 1};
+  plan_subtree(b, leaf_max, plan, 0, spare);
+  out.nnodes_binary = 0;
+  for (uint32_t i = 0; i < N; ++i)
+    if (b.pool[i].count == 0) out.nnodes_binary++;
+  out.root = 0;
+  out.nnodes = b.pool[0].count ? 1u : 1u + plan.below(b, 0);
+  out.nodes.assign((size_t)out.nnodes * kWideWords, 0u);
+  out.tris.assign((size_t)n * 12, 0.f);
+  Emitter em{b, plan, tri9, out, spare};
+  em.run({0, 0, 1, 0, 1});
+  out.nleaves = em.nleaves.load();
+  out.max_depth = em.max_depth.load();
 }
 
 }  // namespace
@@ -419,20 +542,41 @@ int build_bvh(const float *tri9, uint32_t ntri, const ckr_build_params &params, 
   uint32_t threads = params.threads ? params.threads : (hw ? hw : 1);
   b.spare_threads = (int)threads - 1;
 
-  b.prims.reserve(ntri);
-  for (uint32_t i = 0; i < ntri; ++i) {
-    const float *t = tri9 + 9 * (size_t)i;
-    bool finite = true;
-    for (int k = 0; k < 9; ++k) finite = finite && std::isfinite(t[k]);
-    if (!finite) continue;
-    Prim p;
-    p.box.reset();
-    p.box.grow(t);
-    p.box.grow(t + 3);
-    p.box.grow(t + 6);
-    for (int k = 0; k < 3; ++k) p.c[k] = 0.5f * p.box.lo[k] + 0.5f * p.box.hi[k];
-    p.id = i;
-    b.prims.push_back(p);
+  // Primitive boxes, by contiguous ranges on all threads; the ranges' finite
+  // triangles are then concatenated in input order.
+  const uint32_t parts = std::max(1u, std::min(threads, ntri / 65536));
+  std::vector<std::vector<Prim>> part(parts);
+  auto setup = [&](uint32_t k) {
+    const uint32_t lo = (uint32_t)((uint64_t)ntri * k / parts), hi = (uint32_t)((uint64_t)ntri * (k + 1) / parts);
+    std::vector<Prim> &v = part[k];
+    v.reserve(hi - lo);
+    for (uint32_t i = lo; i < hi; ++i) {
+      const float *t = tri9 + 9 * (size_t)i;
+      bool finite = true;
+      for (int c = 0; c < 9; ++c) finite = finite && std::isfinite(t[c]);
+      if (!finite) continue;
+      Prim p;
+      p.box.reset();
+      p.box.grow(t);
+      p.box.grow(t + 3);
+      p.box.grow(t + 6);
+      for (int c = 0; c < 3; ++c) p.c[c] = 0.5f * p.box.lo[c] + 0.5f * p.box.hi[c];
+      p.id = i;
+      v.push_back(p);
+    }
+  };
+  {
+    std::vector<std::thread> ts;
+    for (uint32_t k = 1; k < parts; ++k) ts.emplace_back(setup, k);
+    setup(0);
+    for (std::thread &t : ts) t.join();
+  }
+  size_t total = 0;
+  for (const auto &v : part) total += v.size();
+  b.prims.reserve(total);
+  for (auto &v : part) {
+    b.prims.insert(b.prims.end(), v.begin(), v.end());
+    std::vector<Prim>().swap(v);
   }
   uint32_t n = (uint32_t)b.prims.size();
   out.ntri_indexed = n;
@@ -446,7 +590,7 @@ int build_bvh(const float *tri9, uint32_t ntri, const ckr_build_params &params, 
   for (const Prim &p : b.prims) b.pool[0].box.grow(p.box);
   b.build(0, 0, n);
 
-  collapse(b, tri9, leaf_max, out);
+  collapse(b, tri9, leaf_max, threads, out);
   return validate_bvh(out) ? CKR_OK : CKR_ERR_INVALID_ARGUMENT;
 }
 

@@ -225,3 +225,29 @@ extern "C" int ckr_internal_replay(const float *tri9, uint32_t ntri, uint32_t ma
   if (mean_tris) *mean_tris = n ? (double)T / n : 0.0;
   return CKR_OK;
 }
+
+// Host-only build with an explicit thread count, for the CPU test suite: an FNV-1a
+// digest of the flattened tree (nodes, then triangle records) and its node count,
+// so that builds on different numbers of threads can be compared.  Not part of the
+// public ABI.
+extern "C" int ckr_internal_bvh_digest(const float *tri9, uint32_t ntri, uint32_t max_leaf, uint32_t threads,
+                                       uint64_t *digest, uint32_t *nnodes) {
+  if (!digest || !nnodes) return CKR_ERR_INVALID_ARGUMENT;
+  ckr::FlatBvh bvh;
+  ckr_build_params p{max_leaf, 0, threads};
+  int st = ckr::build_bvh(tri9, ntri, p, bvh);
+  if (st != CKR_OK) return st;
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&h](const void *data, size_t bytes) {
+    const unsigned char *c = static_cast<const unsigned char *>(data);
+    for (size_t i = 0; i < bytes; ++i) {
+      h ^= c[i];
+      h *= 1099511628211ull;
+    }
+  };
+  mix(bvh.nodes.data(), bvh.nodes.size() * sizeof(uint32_t));
+  mix(bvh.tris.data(), bvh.tris.size() * sizeof(float));
+  *digest = h;
+  *nnodes = bvh.nnodes;
+  return CKR_OK;
+}

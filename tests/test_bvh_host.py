@@ -104,3 +104,26 @@ def test_axis_parallel_rays_stay_cheap():
     assert c["edge"] <= 0.03 * n
     # A few nodes per ray, as for random rays; an axis lost to NaN costs hundreds.
     assert nodes < 20, nodes
+
+
+def bvh_digest(tri, threads, leaf=0):
+    L = ckr.lib()
+    f = L.ckr_internal_bvh_digest
+    f.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]
+    f.restype = C.c_int
+    tri = np.ascontiguousarray(tri, dtype=np.float32)
+    h, n = C.c_uint64(), C.c_uint32()
+    assert f(tri.ctypes.data, len(tri), leaf, threads, C.byref(h), C.byref(n)) == 0
+    return h.value, n.value
+
+
+def test_build_is_the_same_on_any_number_of_threads():
+    # 327,680 triangles: the plan and the writing of the wide nodes hand subtrees of
+    # 32,768 or more triangles to other threads (the root's eight children hold
+    # about 40,000 each), and the primitive setup splits into ranges.
+    tri = ckr.icosphere(7, 0.05, 6, 1)
+    one = bvh_digest(tri, 1)
+    assert one[1] > 1000
+    for threads in (2, 3, 8, 16):
+        assert bvh_digest(tri, threads) == one, threads
+    assert bvh_digest(tri, 5, leaf=1) == bvh_digest(tri, 1, leaf=1)

@@ -68,10 +68,27 @@ struct TNode {
 
 struct Builder {
   std::vector<Prim> prims;
-  std::vector<TNode> pool;
+  std::unique_ptr<TNode[]> pool;  // uninitialised: build() writes each node it allocates
   std::atomic<uint32_t> next{1};
   std::atomic<int> spare_threads{0};
-  uint32_t max_leaf = 4, bins = 16;
+  uint32_t max_leaf = 4, bins = 16, threads = 1;
+
+  // Nodes of at least kParallelBin triangles (the top levels, where few subtrees
+  // run at once) compute their centroid bounds, bins and child boxes on `threads`
+  // threads, each over a contiguous range; the partial boxes and counts are merged,
+  // and since min / max and counts do not depend on the order, the result is the
+  // same as on one thread.
+  static constexpr uint32_t kParallelBin = 1u << 18;
+
+  template <class F>
+  void ranges(uint32_t begin, uint32_t end, uint32_t parts, F f) {
+    std::vector<std::thread> ts;
+    for (uint32_t k = 1; k < parts; ++k)
+      ts.emplace_back(f, k, begin + (uint32_t)((uint64_t)(end - begin) * k / parts),
+                      begin + (uint32_t)((uint64_t)(end - begin) * (k + 1) / parts));
+    f(0u, begin, begin + (uint32_t)((uint64_t)(end - begin) / parts));
+    for (std::thread &t : ts) t.join();
+  }
 
   uint32_t alloc2() { return next.fetch_add(2); }
 
@@ -90,9 +107,19 @@ struct Builder {
       make_leaf(node, begin, end);
       return;
     }
+    const uint32_t parts = n >= kParallelBin ? std::max(1u, std::min(threads, n >> 16)) : 1u;
     Box cb;
     cb.reset();
-    for (uint32_t i = begin; i < end; ++i) cb.grow(prims[i].c);
+    if (parts > 1) {
+      std::vector<Box> part(parts);
+      ranges(begin, end, parts, [&](uint32_t k, uint32_t lo, uint32_t hi) {
+        part[k].reset();
+        for (uint32_t i = lo; i < hi; ++i) part[k].grow(prims[i].c);
+      });
+      for (const Box &b : part) cb.grow(b);
+    } else {
+      for (uint32_t i = begin; i < end; ++i) cb.grow(prims[i].c);
+    }
 
     // Binned SAH over the three axes.
     const uint32_t B = bins;
@@ -103,6 +130,28 @@ struct Builder {
     uint32_t bcnt[64];
     float right_area[64];
     uint32_t right_cnt[64];
+    // Large nodes: the bins of all three axes in one pass per thread.
+    std::vector<Box> pbox;
+    std::vector<uint32_t> pcnt;
+    if (parts > 1) {
+      pbox.resize((size_t)parts * 3 * B);
+      pcnt.assign((size_t)parts * 3 * B, 0);
+      ranges(begin, end, parts, [&](uint32_t k, uint32_t lo, uint32_t hi) {
+        Box *bx = &pbox[(size_t)k * 3 * B];
+        uint32_t *ct = &pcnt[(size_t)k * 3 * B];
+        for (uint32_t b = 0; b < 3 * B; ++b) bx[b].reset();
+        for (int axis = 0; axis < 3; ++axis) {
+          const float ext = cb.hi[axis] - cb.lo[axis];
+          if (!(ext > 0.f)) continue;
+          const float scale = (float)B / ext;
+          for (uint32_t i = lo; i < hi; ++i) {
+            const uint32_t b = std::min(B - 1, (uint32_t)((prims[i].c[axis] - cb.lo[axis]) * scale));
+            bx[axis * B + b].grow(prims[i].box);
+            ct[axis * B + b]++;
+          }
+        }
+      });
+    }
     for (int axis = 0; axis < 3; ++axis) {
       float ext = cb.hi[axis] - cb.lo[axis];
       if (!(ext > 0.f)) continue;
@@ -111,10 +160,18 @@ struct Builder {
         bbox[b].reset();
         bcnt[b] = 0;
       }
-      for (uint32_t i = begin; i < end; ++i) {
-        uint32_t b = std::min(B - 1, (uint32_t)((prims[i].c[axis] - cb.lo[axis]) * scale));
-        bbox[b].grow(prims[i].box);
-        bcnt[b]++;
+      if (parts > 1) {
+        for (uint32_t k = 0; k < parts; ++k)
+          for (uint32_t b = 0; b < B; ++b) {
+            bbox[b].grow(pbox[((size_t)k * 3 + axis) * B + b]);
+            bcnt[b] += pcnt[((size_t)k * 3 + axis) * B + b];
+          }
+      } else {
+        for (uint32_t i = begin; i < end; ++i) {
+          uint32_t b = std::min(B - 1, (uint32_t)((prims[i].c[axis] - cb.lo[axis]) * scale));
+          bbox[b].grow(prims[i].box);
+          bcnt[b]++;
+        }
       }
       Box acc;
       acc.reset();
@@ -165,8 +222,22 @@ struct Builder {
     TNode &L = pool[l], &R = pool[l + 1];
     L.box.reset();
     R.box.reset();
-    for (uint32_t i = begin; i < mid; ++i) L.box.grow(prims[i].box);
-    for (uint32_t i = mid; i < end; ++i) R.box.grow(prims[i].box);
+    if (parts > 1) {
+      std::vector<Box> part(2 * (size_t)parts);
+      ranges(begin, end, parts, [&](uint32_t k, uint32_t lo, uint32_t hi) {
+        Box &l = part[2 * k], &r = part[2 * k + 1];
+        l.reset();
+        r.reset();
+        for (uint32_t i = lo; i < hi; ++i) (i < mid ? l : r).grow(prims[i].box);
+      });
+      for (uint32_t k = 0; k < parts; ++k) {
+        L.box.grow(part[2 * k]);
+        R.box.grow(part[2 * k + 1]);
+      }
+    } else {
+      for (uint32_t i = begin; i < mid; ++i) L.box.grow(prims[i].box);
+      for (uint32_t i = mid; i < end; ++i) R.box.grow(prims[i].box);
+    }
     if (n > 65536 && spare_threads.fetch_sub(1) > 0) {
       std::thread t([this, l, begin, mid] { build(l, begin, mid); });
       build(l + 1, mid, end);
@@ -541,6 +612,7 @@ int build_bvh(const float *tri9, uint32_t ntri, const ckr_build_params &params, 
   unsigned hw = std::thread::hardware_concurrency();
   uint32_t threads = params.threads ? params.threads : (hw ? hw : 1);
   b.spare_threads = (int)threads - 1;
+  b.threads = threads;
 
   // Primitive boxes, by contiguous ranges on all threads; the ranges' finite
   // triangles are then concatenated in input order.
@@ -585,7 +657,7 @@ int build_bvh(const float *tri9, uint32_t ntri, const ckr_build_params &params, 
     return CKR_OK;
   }
   if (n >= (1u << 28)) return CKR_ERR_TOO_LARGE;
-  b.pool.resize(2 * (size_t)n + 1);
+  b.pool.reset(new TNode[2 * (size_t)n + 1]);
   b.pool[0].box.reset();
   for (const Prim &p : b.prims) b.pool[0].box.grow(p.box);
   b.build(0, 0, n);

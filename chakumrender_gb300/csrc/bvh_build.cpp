@@ -706,9 +706,19 @@ bool validate_bvh(const FlatBvh &b) {
   }
   for (uint8_t c : covered)
     if (!c) return false;
-  // Bottom-up: exact boxes, and each one inside its quantised slot box.
+  // Bottom-up, deepest level first (a node's children lie one level below it), the
+  // nodes of a level on several threads: exact boxes, and each one inside its
+  // quantised slot box.
   std::vector<float> box((size_t)b.nnodes * 6);
-  for (uint32_t i = b.nnodes; i-- > 0;) {
+  std::vector<uint32_t> order(b.nnodes), first(depth_max + 2, 0);
+  for (uint32_t i = 0; i < b.nnodes; ++i) first[level[i] + 1]++;
+  for (uint32_t l = 1; l <= depth_max + 1; ++l) first[l] += first[l - 1];
+  {
+    std::vector<uint32_t> fill(first.begin(), first.end() - 1);
+    for (uint32_t i = 0; i < b.nnodes; ++i) order[fill[level[i]]++] = i;
+  }
+  std::atomic<bool> ok{true};
+  auto check = [&](uint32_t i) -> bool {
     const uint32_t *w = &b.nodes[(size_t)i * kWideWords];
     const uint32_t imask = w[3] >> 24, child_base = w[4], tri_base = w[5];
     uint8_t meta[8], q[6][8];
@@ -751,6 +761,22 @@ bool validate_bvh(const FlatBvh &b) {
         nb[3 + a] = std::max(nb[3 + a], cb[3 + a]);
       }
     }
+    return true;
+  };
+  const uint32_t hw = std::max(1u, std::thread::hardware_concurrency());
+  for (uint32_t l = depth_max; l >= 1; --l) {
+    const uint32_t lo = first[l], hi = first[l + 1], cnt = hi - lo;
+    const uint32_t parts = std::max(1u, std::min(hw, cnt / 4096));
+    auto run = [&](uint32_t k) {
+      const uint32_t a = lo + (uint32_t)((uint64_t)cnt * k / parts), z = lo + (uint32_t)((uint64_t)cnt * (k + 1) / parts);
+      for (uint32_t j = a; j < z && ok.load(std::memory_order_relaxed); ++j)
+        if (!check(order[j])) ok = false;
+    };
+    std::vector<std::thread> ts;
+    for (uint32_t k = 1; k < parts; ++k) ts.emplace_back(run, k);
+    run(0);
+    for (std::thread &t : ts) t.join();
+    if (!ok) return false;
   }
   return depth_max == b.max_depth && leaves == b.nleaves;
 }

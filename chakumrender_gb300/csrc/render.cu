@@ -46,6 +46,16 @@ struct Workspace {
   DevBuf<float> hit_t;
   DevBuf<double> accum;
   size_t wave = 0, shadow = 0, pixels = 0;
+  uint32_t *h_count = nullptr;  // pinned: queue lengths read back under regeneration
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  Workspace() = default;
+  Workspace(const Workspace &) = delete;
+  Workspace &operator=(const Workspace &) = delete;
+  ~Workspace() {
+    if (h_count) cudaFreeHost(h_count);
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+  }
 };
 
 
@@ -179,67 +189,110 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
                          : cfg->shader == CKR_SHADER_DIRECT_MIS ? (const void *)k_shade<CKR_SHADER_DIRECT_MIS, kRTPB>
                                                                 : (const void *)k_shade_miscv<kRTPB>;
   const int g_shade = grid_for(shade_fn, cfg->shader == CKR_SHADER_EXPLICIT ? smem : 0, kRTPB);
-  for (uint64_t base = 0; base < total; base += wave) {
-    uint32_t n = (uint32_t)std::min<uint64_t>(wave, total - base);
-    k_camera<kRTPB><<<std::min<int>(g_ext, ceil_div(n, kRTPB)), kRTPB, 0, stream>>>(c, P, prm, base, n);
-    int cur = 0;
-    for (uint32_t d = 0; d <= prm.max_depth; ++d) {
-      // Work counters of k_extend and k_shadow (P.counts[3], [4]).
-      CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 3, 0, 2 * sizeof(uint32_t), stream));
-      extend_fn<<<g_ext, kRTPB, smem, stream>>>(sv, P, cur, depth);
-      CKR_CUDA_TRY(cudaMemsetAsync(P.counts + (cur ^ 1), 0, sizeof(uint32_t), stream));
-      CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), stream));
-      Learn lr{};
-      // Vertices at the last depth only add emission: no light sample, so neither
-      // a light distribution nor training records there.
-      const bool nee = d < prm.max_depth;
-      if (prop) lr.sel_prev = d ? prop->sel[(d - 1) & 1].ptr : nullptr;
-      if (prop && nee) {
-        // Light distributions at this bounce's vertices.
-        mlp::PathRows pr;
-        pr.queue = cur ? P.q1 : P.q0;
-        pr.hit_id = P.hit_id;
-        pr.ray_o = P.ray_o;
-        pr.ray_d = P.ray_d;
-        pr.hit_t = P.hit_t;
-        pr.meta = P.meta;
-        pr.sv = shv;
-        int ms = mlp::infer_paths(prop->net, pr, (uint32_t)wave, P.counts + cur, prop->sel[d & 1].ptr,
-                                  prop->defensive, stream);
-        if (ms != CKR_OK) return ms;
-        lr.sel = prop->sel[d & 1].ptr;
-        if (train) {
-          lr.rec = prop->rec.ptr;
-          lr.rec_count = prop->rec_count.ptr;
-          lr.rec_cap = prop->batch;
-        }
+  // One step of the wavefront over queue `cur`: closest hit, [learned selection],
+  // shading, shadow rays, [training].  k: the step's index within the wave (or the
+  // render, with regeneration) -- it picks the selection buffer, and k = 0 has no
+  // previous one; nee: the step's vertices may draw light samples.
+  int cur = 0;
+  auto step = [&](uint64_t k, bool nee) -> int {
+    // Work counters of k_extend and k_shadow (P.counts[3], [4]).
+    CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 3, 0, 2 * sizeof(uint32_t), stream));
+    extend_fn<<<g_ext, kRTPB, smem, stream>>>(sv, P, cur, depth);
+    CKR_CUDA_TRY(cudaMemsetAsync(P.counts + (cur ^ 1), 0, sizeof(uint32_t), stream));
+    CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), stream));
+    Learn lr{};
+    if (prop) lr.sel_prev = k ? prop->sel[(k - 1) & 1].ptr : nullptr;
+    if (prop && nee) {
+      // Light distributions at this step's vertices.
+      mlp::PathRows pr;
+      pr.queue = cur ? P.q1 : P.q0;
+      pr.hit_id = P.hit_id;
+      pr.ray_o = P.ray_o;
+      pr.ray_d = P.ray_d;
+      pr.hit_t = P.hit_t;
+      pr.meta = P.meta;
+      pr.sv = shv;
+      int ms = mlp::infer_paths(prop->net, pr, (uint32_t)wave, P.counts + cur, prop->sel[k & 1].ptr,
+                                prop->defensive, stream);
+      if (ms != CKR_OK) return ms;
+      lr.sel = prop->sel[k & 1].ptr;
+      if (train) {
+        lr.rec = prop->rec.ptr;
+        lr.rec_count = prop->rec_count.ptr;
+        lr.rec_cap = prop->batch;
       }
-      if (cfg->shader == CKR_SHADER_EXPLICIT)
-        k_shade<CKR_SHADER_EXPLICIT, kRTPB><<<g_shade, kRTPB, smem, stream>>>(shv, P, prm, cur, (int)d, ltc, sv, depth);
-      else if (cfg->shader == CKR_SHADER_PATH_NEE)
-        k_shade_nee<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, lr);
-      else if (cfg->shader == CKR_SHADER_PATH)
-        k_shade_path<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
-      else if (cfg->shader == CKR_SHADER_DIRECT_CV)
-        k_shade<CKR_SHADER_DIRECT_CV, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
-      else if (cfg->shader == CKR_SHADER_DIRECT_MIS)
-        k_shade<CKR_SHADER_DIRECT_MIS, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
-      else
-        k_shade_miscv<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
-      shadow_fn<<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur, train && nee ? prop->rec.ptr : nullptr);
-      if (train && nee) {
-        // Adam steps on this bounce's light samples (visibility applied above),
-        // minibatch by minibatch; steps past the records actually written are no-ops.
-        for (uint32_t off = 0; off < prop->batch; off += prop->minibatch) {
-          int ts = mlp::train_step(prop->net, prop->rec.ptr + 3 * (size_t)off,
-                                   std::min(prop->minibatch, prop->batch - off), prop->rec_count.ptr, off, stream);
-          if (ts != CKR_OK) return ts;
-        }
-        CKR_CUDA_TRY(cudaMemsetAsync(prop->rec_count.ptr, 0, 4, stream));
-        if (prop->max_steps && prop->net.step >= prop->max_steps) train = false;  // converged: inference only
+    }
+    const int d = (int)std::min<uint64_t>(k, prm.max_depth);
+    if (cfg->shader == CKR_SHADER_EXPLICIT)
+      k_shade<CKR_SHADER_EXPLICIT, kRTPB><<<g_shade, kRTPB, smem, stream>>>(shv, P, prm, cur, d, ltc, sv, depth);
+    else if (cfg->shader == CKR_SHADER_PATH_NEE)
+      k_shade_nee<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, lr);
+    else if (cfg->shader == CKR_SHADER_PATH)
+      k_shade_path<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, d, ltc);
+    else if (cfg->shader == CKR_SHADER_DIRECT_CV)
+      k_shade<CKR_SHADER_DIRECT_CV, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, d, ltc);
+    else if (cfg->shader == CKR_SHADER_DIRECT_MIS)
+      k_shade<CKR_SHADER_DIRECT_MIS, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, d, ltc);
+    else
+      k_shade_miscv<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, d, ltc);
+    shadow_fn<<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur, train && nee ? prop->rec.ptr : nullptr);
+    if (train && nee) {
+      // Adam steps on this step's light samples (visibility applied above),
+      // minibatch by minibatch; steps past the records actually written are no-ops.
+      for (uint32_t off = 0; off < prop->batch; off += prop->minibatch) {
+        int ts = mlp::train_step(prop->net, prop->rec.ptr + 3 * (size_t)off,
+                                 std::min(prop->minibatch, prop->batch - off), prop->rec_count.ptr, off, stream);
+        if (ts != CKR_OK) return ts;
       }
-      cur ^= 1;
-      if (!path) break;
+      CKR_CUDA_TRY(cudaMemsetAsync(prop->rec_count.ptr, 0, 4, stream));
+      if (prop->max_steps && prop->net.step >= prop->max_steps) train = false;  // converged: inference only
+    }
+    cur ^= 1;
+    return CKR_OK;
+  };
+  // Path regeneration for path tracers of more than one wave (outside stream
+  // capture, whose launch sequence must be fixed): one wave of slots, and a
+  // shading step that ends a path starts the next camera path in its slot, so
+  // every step runs a full queue until the last paths have started.  The host
+  // stops when the queue is empty, reading its length one step behind so that the
+  // device always has the next step queued.
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  CKR_CUDA_TRY(cudaStreamIsCapturing(stream, &capture));
+  const bool regen = (cfg->shader == CKR_SHADER_PATH || cfg->shader == CKR_SHADER_PATH_NEE) && total > wave &&
+                     capture == cudaStreamCaptureStatusNone && total + 64ull * wave < (1ull << 32);
+  if (regen) {
+    if (!W.h_count) CKR_CUDA_TRY(cudaMallocHost((void **)&W.h_count, 2 * sizeof(uint32_t)));
+    for (cudaEvent_t &e : W.ev)
+      if (!e) CKR_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    prm.regen_total = (uint32_t)total;
+    prm.cam = c;
+    k_camera<kRTPB><<<std::min<int>(g_ext, ceil_div(wave, kRTPB)), kRTPB, 0, stream>>>(c, P, prm, 0, (uint32_t)wave);
+    // While paths start, every step runs `wave` vertices, and a path has at most
+    // max_depth + 1: a bound on the steps in case the read-back never sees zero.
+    const uint64_t max_steps = ceil_div(total, wave) * (uint64_t)(prm.max_depth + 1) + prm.max_depth + 2;
+    for (uint64_t k = 0; k < max_steps; ++k) {
+      int st = step(k, true);
+      if (st != CKR_OK) return st;
+      CKR_CUDA_TRY(cudaMemcpyAsync(W.h_count + (k & 1), P.counts + cur, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                   stream));
+      CKR_CUDA_TRY(cudaEventRecord(W.ev[k & 1], stream));
+      if (k >= 1) {
+        CKR_CUDA_TRY(cudaEventSynchronize(W.ev[(k - 1) & 1]));
+        if (W.h_count[(k - 1) & 1] == 0) break;
+      }
+    }
+  } else {
+    for (uint64_t base = 0; base < total; base += wave) {
+      uint32_t n = (uint32_t)std::min<uint64_t>(wave, total - base);
+      k_camera<kRTPB><<<std::min<int>(g_ext, ceil_div(n, kRTPB)), kRTPB, 0, stream>>>(c, P, prm, base, n);
+      cur = 0;
+      for (uint32_t d = 0; d <= prm.max_depth; ++d) {
+        // The vertices at the last depth only add emission: no light sample, so
+        // neither a light distribution nor training records there.
+        int st = step(d, d < prm.max_depth);
+        if (st != CKR_OK) return st;
+        if (!path) break;
+      }
     }
   }
   uint32_t n3 = prm.npix * 3;

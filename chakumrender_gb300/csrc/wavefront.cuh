@@ -90,6 +90,11 @@ struct Params {
   uint32_t shadow_per_path;
   const JobDev *jobs;  // batched render (nullptr: one render described by the fields above)
   uint32_t njobs;
+  // Path regeneration (single render): a shading kernel that ends a path starts
+  // camera path P.counts[5]++ in its slot while that index is below regen_total
+  // (0: off); cam is the camera of those paths.
+  uint32_t regen_total;
+  Cam cam;
 };
 
 // Per-path values that a batch takes from the path's job.
@@ -148,35 +153,57 @@ __device__ __forceinline__ void add_px(double *accum, uint32_t px, F3 c) {
   atomicAdd(&accum[3 * (size_t)px + 2], (double)c.z);
 }
 
+// Starts camera path g (path index = sample * npix + pixel, within a job) in path
+// slot `slot`.
+__device__ __forceinline__ void camera_path(const Cam &cam0, const Params &prm, const Paths &P, uint64_t g,
+                                            uint32_t slot) {
+  Cam cam = cam0;
+  uint32_t npix = prm.npix, job = 0, px_base = 0;
+  if (prm.jobs) {
+    job = job_of(prm.jobs, prm.njobs, g);
+    const JobDev &J = prm.jobs[job];
+    cam = J.cam;
+    npix = J.npix;
+    px_base = J.accum_off;
+    g -= J.path_begin;
+  }
+  uint32_t sample = (uint32_t)(g / npix), pix = (uint32_t)(g % npix);
+  uint32_t x = pix % cam.w, y = pix / cam.w;
+  float jx = sample < 8 ? c_jx[sample] : 0.f, jy = sample < 8 ? c_jy[sample] : 0.f;
+  F3 d = cam.cx * (((float)x + jx) / (float)cam.w - 0.5f) + cam.cy * (((float)y + jy) / (float)cam.h - 0.5f) +
+         cam.dir;
+  d = normalize(d);
+  P.ray_o[slot] = make_float4(cam.pos.x, cam.pos.y, cam.pos.z, 0.f);
+  P.ray_d[slot] = make_float4(d.x, d.y, d.z, 3.0e38f);
+  P.beta[slot] = make_float4(1.f, 1.f, 1.f, 1.f);
+  uint32_t out_px = (cam.h - 1 - y) * cam.w + x;
+  P.meta[slot] = make_uint4(px_base + out_px, sample, 0u, job << 8);
+}
+
+// Camera paths wave_base + [0, wave_n) into slots [0, wave_n) and queue 0; the
+// next path to start (regeneration) is wave_base + wave_n.
 template <int TPB>
 __global__ void __launch_bounds__(TPB) k_camera(Cam cam0, Paths P, Params prm, uint64_t wave_base,
                                                   uint32_t wave_n) {
   for (uint32_t i = blockIdx.x * TPB + threadIdx.x; i < wave_n; i += gridDim.x * TPB) {
-    uint64_t g = wave_base + i;  // path index = sample * npix + pixel (within a job)
-    Cam cam = cam0;
-    uint32_t npix = prm.npix, job = 0, px_base = 0;
-    if (prm.jobs) {
-      job = job_of(prm.jobs, prm.njobs, g);
-      const JobDev &J = prm.jobs[job];
-      cam = J.cam;
-      npix = J.npix;
-      px_base = J.accum_off;
-      g -= J.path_begin;
-    }
-    uint32_t sample = (uint32_t)(g / npix), pix = (uint32_t)(g % npix);
-    uint32_t x = pix % cam.w, y = pix / cam.w;
-    float jx = sample < 8 ? c_jx[sample] : 0.f, jy = sample < 8 ? c_jy[sample] : 0.f;
-    F3 d = cam.cx * (((float)x + jx) / (float)cam.w - 0.5f) + cam.cy * (((float)y + jy) / (float)cam.h - 0.5f) +
-           cam.dir;
-    d = normalize(d);
-    P.ray_o[i] = make_float4(cam.pos.x, cam.pos.y, cam.pos.z, 0.f);
-    P.ray_d[i] = make_float4(d.x, d.y, d.z, 3.0e38f);
-    P.beta[i] = make_float4(1.f, 1.f, 1.f, 1.f);
-    uint32_t out_px = (cam.h - 1 - y) * cam.w + x;
-    P.meta[i] = make_uint4(px_base + out_px, sample, 0u, job << 8);
+    camera_path(cam0, prm, P, wave_base + i, i);
     P.q0[i] = i;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) P.counts[0] = wave_n;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.counts[0] = wave_n;
+    P.counts[5] = (uint32_t)(wave_base + wave_n);
+  }
+}
+
+// Path regeneration at the end of a shading step: lanes whose path ended take the
+// next camera paths (one warp-wide reservation).  Returns true when this lane's
+// slot now holds a fresh camera path.  All 32 lanes must call.
+__device__ __forceinline__ bool regenerate(const Params &prm, const Paths &P, bool ended, uint32_t slot) {
+  if (!prm.regen_total) return false;
+  const uint32_t g = warp_reserve(&P.counts[5], ended ? 1u : 0u);
+  if (!ended || g >= prm.regen_total) return false;
+  camera_path(prm.cam, prm, P, g, slot);
+  return true;
 }
 
 // Trees at least this many levels deep are traversed with dynamic fetching
@@ -632,7 +659,8 @@ __device__ __forceinline__ void shade(ShadeView sv0, Paths P, Params prm, int cu
         }
       }
     }
-    uint32_t cbase = warp_reserve(&P.counts[cur ^ 1], cont ? 1u : 0u);
+    const bool fresh = regenerate(prm, P, valid && !cont, slot);
+    uint32_t cbase = warp_reserve(&P.counts[cur ^ 1], cont || fresh ? 1u : 0u);
     if (cont) {
       // Continue in place: the path keeps its slot.  tmin = -1 marks a ray the
       // explicit loop has traced already.
@@ -641,8 +669,8 @@ __device__ __forceinline__ void shade(ShadeView sv0, Paths P, Params prm, int cu
       P.beta[slot] = next_b;
       uint32_t nd = meta.z + 1;
       P.meta[slot] = make_uint4(meta.x, meta.y, nd, (meta.w & ~1u) | (nd >= pc.max_depth ? 1u : 0u));
-      qn[cbase] = slot;
     }
+    if (cont || fresh) qn[cbase] = slot;
   }
 }
 
@@ -823,7 +851,8 @@ __global__ void __launch_bounds__(TPB, (640 / TPB > 1 ? 640 / TPB : 1))
       P.sh_px[sbase] = meta.x;
       if (lr.rec) P.sh_rec[sbase] = rbase;
     }
-    uint32_t cbase = warp_reserve(&P.counts[cur ^ 1], cont ? 1u : 0u);
+    const bool fresh = regenerate(prm, P, valid && !cont, slot);
+    uint32_t cbase = warp_reserve(&P.counts[cur ^ 1], cont || fresh ? 1u : 0u);
     if (cont) {
       P.ray_o[slot] = make_float4(next_o.x, next_o.y, next_o.z, 0.f);
       P.ray_d[slot] = next_d;
@@ -831,8 +860,8 @@ __global__ void __launch_bounds__(TPB, (640 / TPB > 1 ? 640 / TPB : 1))
       uint32_t nd = meta.z + 1;
       P.meta[slot] = make_uint4(meta.x, meta.y, nd, (meta.w & ~1u) | (nd >= pc.max_depth ? 1u : 0u));
       if (lr.sel) P.prev_row[slot] = i;
-      qn[cbase] = slot;
     }
+    if (cont || fresh) qn[cbase] = slot;
   }
 }
 

@@ -45,6 +45,23 @@ def test_noalloc_matches_render(torch_cuda, shader, spp, nl, nb, depth):
         assert np.allclose(img, ref, rtol=1e-6, atol=1e-7)
 
 
+@pytest.mark.parametrize("shader", [S.SHADER_PATH, S.SHADER_PATH_NEE])
+def test_regenerating_render_matches_waves(torch_cuda, shader):
+    """A path-tracer render of more than one wave of paths (here 4,194,304 against 2^21
+    slots) starts a new camera path in the slot of every path that ends; the same paths
+    rendered in fixed waves of 32,768 (ckr_render_noalloc) give the same image."""
+    sd = S.load_xml(S.SCENES / "box.xml")
+    cam = sd.camera
+    cam.width = cam.height = 512
+    cfg = S.render_cfg(shader=shader, spp=16, n_light=1, n_brdf=1, max_depth=5)
+    scene = S.RenderScene(sd)
+    ref = scene.render_host(cam, cfg)
+    st, img = noalloc(scene, cam, cfg, torch_cuda)
+    assert st == 0
+    assert np.all(np.isfinite(ref)) and ref.mean() > 0
+    assert np.allclose(img, ref, rtol=1e-6, atol=1e-7)
+
+
 def test_noalloc_rejects_oversized_images(torch_cuda):
     sd = S.load_xml(S.SCENES / "box.xml")
     cam = sd.camera

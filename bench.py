@@ -312,7 +312,7 @@ def bench_manylight(torch):
     t_plain = timed(lambda: scene.render(cam, cfg(SPP, 2), rgb.data_ptr()))
     closest, shadow = scene.ray_stats(reset=True)
     e_plain = rel_mse()
-    opts = dict(minibatch=4096, max_steps=1000, lr=3e-3)
+    opts = dict(minibatch=4096, max_steps=1000, lr=3e-3, batch=262144)
     cold = Proposal(scene, seed=1, **opts)
     t_cold64 = timed(lambda: cold.render(cam, cfg(SPP, 3), rgb.data_ptr()))
     e_cold64 = rel_mse()
@@ -344,7 +344,8 @@ def bench_manylight(torch):
                                                            "warm": round(e_plain / e_warm, 3)},
             "reference": {"spp": 16384, "window": [X0, Y0, CW, CH], "sec": round(ref_sec, 2),
                           "accumulation": "fp64"},
-            "proposal": {"minibatch": opts["minibatch"], "max_steps": opts["max_steps"], "defensive": 0.2,
+            "proposal": {"minibatch": opts["minibatch"], "batch": opts["batch"], "max_steps": opts["max_steps"],
+                         "defensive": 0.2,
                          "lr": opts["lr"]}}
 
 

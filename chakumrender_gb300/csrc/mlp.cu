@@ -217,13 +217,14 @@ struct SmemInfer {
   int abort[kGroups];
 };
 
-// A queue entry's path state, gathered in two dependent steps (the path slot from the
-// queue, then the slot's hit and ray) so that each step's latency can overlap other
-// work of the tile before it.
+// A queue entry's path state, gathered in three dependent steps (the path slot from
+// the queue, the slot's hit and ray, the hit triangle's normal and alpha) so that
+// each step's latency can overlap other work of the tile before it.
 struct PathGather {
   uint32_t slot, id, flags;
   float4 ro, rd;
   float t;
+  float4 na;
 };
 
 __device__ __forceinline__ void gather_slot(const PathRows &pr, uint32_t row, uint32_t n, PathGather &g) {
@@ -240,12 +241,28 @@ __device__ __forceinline__ void gather_hit(const PathRows &pr, PathGather &g) {
   g.t = pr.hit_t[g.slot];
 }
 
+// The hit triangle's normal and material alpha from the per-triangle table (a third
+// dependent step).
+__device__ __forceinline__ void gather_na(const PathRows &pr, PathGather &g) {
+  if (pr.tri_na && g.id != kMiss && !(g.id & kSphereBit)) g.na = pr.tri_na[g.id];
+}
+
 // Network input of a gathered queue entry: its shading point (zeros where the entry is
 // not a shaded surface).
 __device__ __forceinline__ void path_row(const PathRows &pr, const PathGather &g, float4 &r0, float4 &r1,
                                          float4 &r2) {
   r0 = r1 = r2 = make_float4(0, 0, 0, 0);
   if (g.id == kMiss || (g.flags & 1u)) return;
+  if (pr.tri_na && !(g.id & kSphereBit)) {
+    if (g.na.w < 0.f) return;  // an emitter
+    const F3 d = f3(g.rd.x, g.rd.y, g.rd.z), x = f3(g.ro.x, g.ro.y, g.ro.z) + d * g.t;
+    F3 nn = f3(g.na.x, g.na.y, g.na.z);
+    if (dot(d, nn) > 0.f) nn = -nn;
+    r0 = make_float4(x.x, x.y, x.z, g.na.w);
+    r1 = make_float4(nn.x, nn.y, nn.z, 0.f);
+    r2 = make_float4(-d.x, -d.y, -d.z, 0.f);
+    return;
+  }
   Surface S = make_surface(pr.sv, f3(g.ro.x, g.ro.y, g.ro.z), f3(g.rd.x, g.rd.y, g.rd.z), g.id, g.t);
   const ckr_material &mm = pr.sv.mats[S.mat];
   if (mm.light_type != 0) return;
@@ -255,7 +272,7 @@ __device__ __forceinline__ void path_row(const PathRows &pr, const PathGather &g
 }
 
 template <bool PATHS>
-__global__ void __launch_bounds__(kInferTPB) k_mlp_infer(const float4 *__restrict__ rec, PathRows pr, uint32_t n_max,
+__global__ void __launch_bounds__(kInferTPB, 2) k_mlp_infer(const float4 *__restrict__ rec, PathRows pr, uint32_t n_max,
                                                          const uint32_t *n_dev, uint32_t n_off,
                                                          const uint8_t *__restrict__ img, Params p, float delta,
                                                          __half *__restrict__ probs, uint16_t *__restrict__ cdf16,
@@ -282,12 +299,15 @@ __global__ void __launch_bounds__(kInferTPB) k_mlp_infer(const float4 *__restric
   uint32_t phase = 0;
   const uint32_t stride = gridDim.x * kGroups;
   // PATHS: the gather of the next tile's rows runs one tile ahead -- its queue load
-  // during this tile's MMA chain, its hit and ray loads during this tile's softmax --
-  // leaving only the triangle and material loads of make_surface exposed.
+  // from the start of this tile's MMA chain, its hit and ray loads from the second
+  // layer, its triangle's normal and alpha (PathRows::tri_na) during the softmax --
+  // so that a row's inputs are in registers when its tile starts (spheres still
+  // read the scene through make_surface).  Two CTAs per SM: 128 registers.
   PathGather cur{}, nxt{};
   if (PATHS) {
     gather_slot(pr, (blockIdx.x * kGroups + g) * 128u + t, n, cur);
     gather_hit(pr, cur);
+    gather_na(pr, cur);
   }
   for (uint32_t tile = blockIdx.x * kGroups + g; tile * 128u < n; tile += stride) {
     const uint32_t row = tile * 128u + t;
@@ -312,9 +332,10 @@ __global__ void __launch_bounds__(kInferTPB) k_mlp_infer(const float4 *__restric
       }
       ok = wait_mma(g, mbar, phase, &S.abort[g], err);
       if (ok && l < 3) epilogue_relu(lane_addr, A, t);
+      if (PATHS && l == 1) gather_hit(pr, nxt);
     }
     if (!ok) break;
-    if (PATHS) gather_hit(pr, nxt);
+    if (PATHS) gather_na(pr, nxt);
     float e[64];
     const bool full = p.nclusters == 64;
     const float sum = full ? softmax_exp64(lane_addr, e) : softmax_exp(lane_addr, p.nclusters, e);

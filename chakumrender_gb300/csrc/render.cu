@@ -38,6 +38,18 @@ uint32_t mesh_lights_of(const ckr_scene *s) {
   return n;
 }
 
+// Per triangle: the geometric normal as make_surface computes it, and the material's
+// alpha (-1 for an emitter), the learned selection's inputs besides the ray.
+__global__ void k_tri_na(ShadeView sv, uint32_t ntri, float4 *out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ntri) return;
+  const float *t9 = sv.tri9 + 9 * (size_t)i;
+  const F3 A = f3(t9[0], t9[1], t9[2]), B = f3(t9[3], t9[4], t9[5]), C = f3(t9[6], t9[7], t9[8]);
+  const F3 n = normalize(cross_rn(C - A, B - A));
+  const ckr_material &m = sv.mats[sv.tri_mat[i]];
+  out[i] = make_float4(n.x, n.y, n.z, m.light_type != 0 ? -1.f : m.alpha);
+}
+
 struct Workspace {
   DevBuf<float4> ray_o, ray_d, beta, sh_o, sh_d, sh_c;
   DevBuf<uint4> meta;
@@ -147,6 +159,12 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   P.stats = W.stats.ptr;
   P.accum = acc;
   bool train = prop && prop->train && (!prop->max_steps || prop->net.step < prop->max_steps);
+  if (prop && !s->tri_na.ptr && s->ntri) {
+    // The network's per-triangle inputs, built once per scene.
+    CKR_CUDA_TRY(s->tri_na.reserve(s->ntri));
+    k_tri_na<<<ceil_div(s->ntri, 256), 256, 0, stream>>>(shade_view_of(s), s->ntri, s->tri_na.ptr);
+    CKR_CUDA_TRY(cudaGetLastError());
+  }
   if (prop) {
     CKR_CUDA_TRY(prop->sel[0].reserve(64 * wave));
     CKR_CUDA_TRY(prop->sel[1].reserve(64 * wave));
@@ -212,6 +230,7 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
       pr.hit_t = P.hit_t;
       pr.meta = P.meta;
       pr.sv = shv;
+      pr.tri_na = s->tri_na.ptr;
       int ms = mlp::infer_paths(prop->net, pr, (uint32_t)wave, P.counts + cur, prop->sel[k & 1].ptr,
                                 prop->defensive, stream);
       if (ms != CKR_OK) return ms;

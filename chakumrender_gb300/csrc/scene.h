@@ -72,6 +72,7 @@ struct ckr_scene {
   ckr::DevBuf<ckr_material> mats;
   ckr::DevBuf<uint32_t> tri_mat, sph_mat, cdf;
   ckr::DevBuf<float> tri9;
+  ckr::DevBuf<float4> tri_na;  // per triangle: geometric normal, material alpha (-1: emitter)
   ckr::DevBuf<ckr::DevLight> lights;
   ckr::DevBuf<uint32_t> tri_light;
   ckr::DevBuf<float> pcdf, sel_cdf;

@@ -241,10 +241,10 @@ __device__ __forceinline__ void gather_hit(const PathRows &pr, PathGather &g) {
   g.t = pr.hit_t[g.slot];
 }
 
-// The hit triangle's normal and material alpha from the per-triangle table (a third
+// The hit triangle's normal and material index (ShadeView::tri_nm, a third
 // dependent step).
 __device__ __forceinline__ void gather_na(const PathRows &pr, PathGather &g) {
-  if (pr.tri_na && g.id != kMiss && !(g.id & kSphereBit)) g.na = pr.tri_na[g.id];
+  if (g.id != kMiss && !(g.id & kSphereBit)) g.na = pr.sv.tri_nm[g.id];
 }
 
 // Network input of a gathered queue entry: its shading point (zeros where the entry is
@@ -253,12 +253,13 @@ __device__ __forceinline__ void path_row(const PathRows &pr, const PathGather &g
                                          float4 &r2) {
   r0 = r1 = r2 = make_float4(0, 0, 0, 0);
   if (g.id == kMiss || (g.flags & 1u)) return;
-  if (pr.tri_na && !(g.id & kSphereBit)) {
-    if (g.na.w < 0.f) return;  // an emitter
+  if (!(g.id & kSphereBit)) {
+    const ckr_material &mm = pr.sv.mats[__float_as_uint(g.na.w)];
+    if (mm.light_type != 0) return;  // an emitter
     const F3 d = f3(g.rd.x, g.rd.y, g.rd.z), x = f3(g.ro.x, g.ro.y, g.ro.z) + d * g.t;
     F3 nn = f3(g.na.x, g.na.y, g.na.z);
     if (dot(d, nn) > 0.f) nn = -nn;
-    r0 = make_float4(x.x, x.y, x.z, g.na.w);
+    r0 = make_float4(x.x, x.y, x.z, mm.alpha);
     r1 = make_float4(nn.x, nn.y, nn.z, 0.f);
     r2 = make_float4(-d.x, -d.y, -d.z, 0.f);
     return;
@@ -300,7 +301,7 @@ __global__ void __launch_bounds__(kInferTPB, 2) k_mlp_infer(const float4 *__rest
   const uint32_t stride = gridDim.x * kGroups;
   // PATHS: the gather of the next tile's rows runs one tile ahead -- its queue load
   // from the start of this tile's MMA chain, its hit and ray loads from the second
-  // layer, its triangle's normal and alpha (PathRows::tri_na) during the softmax --
+  // layer, its triangle's normal and material (ShadeView::tri_nm) during the softmax --
   // so that a row's inputs are in registers when its tile starts (spheres still
   // read the scene through make_surface).  Two CTAs per SM: 128 registers.
   PathGather cur{}, nxt{};

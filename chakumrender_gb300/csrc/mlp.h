@@ -24,7 +24,6 @@ struct PathRows {
   const float4 *ray_o = nullptr, *ray_d = nullptr;
   const float *hit_t = nullptr;
   const uint4 *meta = nullptr;
-  const float4 *tri_na = nullptr;  // per triangle: normal, alpha (< 0: emitter); null: from the scene
   ShadeView sv{};
 };
 

@@ -38,16 +38,17 @@ uint32_t mesh_lights_of(const ckr_scene *s) {
   return n;
 }
 
-// Per triangle: the geometric normal as make_surface computes it, and the material's
-// alpha (-1 for an emitter), the learned selection's inputs besides the ray.
-__global__ void k_tri_na(ShadeView sv, uint32_t ntri, float4 *out) {
+// Per triangle: the geometric normal and the material index, which a surface hit
+// needs (make_surface) -- one 16-byte load instead of nine vertex loads and a
+// dependent material load.
+__global__ void k_tri_nm(const float *__restrict__ tri9, const uint32_t *__restrict__ tri_mat, uint32_t ntri,
+                         float4 *out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ntri) return;
-  const float *t9 = sv.tri9 + 9 * (size_t)i;
+  const float *t9 = tri9 + 9 * (size_t)i;
   const F3 A = f3(t9[0], t9[1], t9[2]), B = f3(t9[3], t9[4], t9[5]), C = f3(t9[6], t9[7], t9[8]);
   const F3 n = normalize(cross_rn(C - A, B - A));
-  const ckr_material &m = sv.mats[sv.tri_mat[i]];
-  out[i] = make_float4(n.x, n.y, n.z, m.light_type != 0 ? -1.f : m.alpha);
+  out[i] = make_float4(n.x, n.y, n.z, __uint_as_float(tri_mat[i]));
 }
 
 struct Workspace {
@@ -159,12 +160,6 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   P.stats = W.stats.ptr;
   P.accum = acc;
   bool train = prop && prop->train && (!prop->max_steps || prop->net.step < prop->max_steps);
-  if (prop && !s->tri_na.ptr && s->ntri) {
-    // The network's per-triangle inputs, built once per scene.
-    CKR_CUDA_TRY(s->tri_na.reserve(s->ntri));
-    k_tri_na<<<ceil_div(s->ntri, 256), 256, 0, stream>>>(shade_view_of(s), s->ntri, s->tri_na.ptr);
-    CKR_CUDA_TRY(cudaGetLastError());
-  }
   if (prop) {
     CKR_CUDA_TRY(prop->sel[0].reserve(64 * wave));
     CKR_CUDA_TRY(prop->sel[1].reserve(64 * wave));
@@ -230,7 +225,6 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
       pr.hit_t = P.hit_t;
       pr.meta = P.meta;
       pr.sv = shv;
-      pr.tri_na = s->tri_na.ptr;
       int ms = mlp::infer_paths(prop->net, pr, (uint32_t)wave, P.counts + cur, prop->sel[k & 1].ptr,
                                 prop->defensive, stream);
       if (ms != CKR_OK) return ms;
@@ -542,3 +536,14 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
   CKR_CUDA_TRY(cudaGetLastError());
   return CKR_OK;
 }
+
+namespace ckr {
+int build_tri_nm(ckr_scene *s) {
+  if (s->ntri == 0) return CKR_OK;
+  CKR_CUDA_TRY(s->tri_nm.reserve(s->ntri));
+  k_tri_nm<<<ceil_div(s->ntri, 256), 256>>>(s->tri9.ptr, s->tri_mat.ptr, s->ntri, s->tri_nm.ptr);
+  CKR_CUDA_TRY(cudaGetLastError());
+  CKR_CUDA_TRY(cudaDeviceSynchronize());
+  return CKR_OK;
+}
+}  // namespace ckr

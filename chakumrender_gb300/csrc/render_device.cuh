@@ -61,12 +61,11 @@ __device__ __forceinline__ Surface make_surface(const ShadeView &sv, F3 o, F3 d,
     n = normalize(f3(c.x, c.y, c.z) - s.x);
     s.mat = __ldg(&sv.sph_mat[j]);
   } else {
-    const float *t9 = sv.tri9 + 9 * (size_t)id;
-    F3 A = f3(__ldg(t9), __ldg(t9 + 1), __ldg(t9 + 2));
-    F3 B = f3(__ldg(t9 + 3), __ldg(t9 + 4), __ldg(t9 + 5));
-    F3 C = f3(__ldg(t9 + 6), __ldg(t9 + 7), __ldg(t9 + 8));
-    n = normalize(cross_rn(C - A, B - A));
-    s.mat = __ldg(&sv.tri_mat[id]);
+    // normalize(cross_rn(C - A, B - A)) of the vertices and the material, one load
+    // (ShadeView::tri_nm).
+    const float4 nm = __ldg(&sv.tri_nm[id]);
+    n = f3(nm.x, nm.y, nm.z);
+    s.mat = __float_as_uint(nm.w);
   }
   if (dot(d, n) > 0.f) n = -n;
   s.n = n;

@@ -34,7 +34,8 @@ constexpr uint32_t kInvCdfBins = 300;  // MeshLight::invCDFBins (headers/lightSo
 struct ShadeView {
   const ckr_material *mats;
   const uint32_t *tri_mat;   // per input triangle
-  const float *tri9;         // input-order vertices (shading normals, light sampling)
+  const float *tri9;         // input-order vertices (light sampling)
+  const float4 *tri_nm;      // per input triangle: geometric normal, material index (bits)
   const uint32_t *sph_mat;
   const float4 *sph;         // centre, radius
   const DevLight *lights;     // sorted: sphere, mesh, triangle, point lights
@@ -72,7 +73,7 @@ struct ckr_scene {
   ckr::DevBuf<ckr_material> mats;
   ckr::DevBuf<uint32_t> tri_mat, sph_mat, cdf;
   ckr::DevBuf<float> tri9;
-  ckr::DevBuf<float4> tri_na;  // per triangle: geometric normal, material alpha (-1: emitter)
+  ckr::DevBuf<float4> tri_nm;  // per triangle: geometric normal, material index (bits)
   ckr::DevBuf<ckr::DevLight> lights;
   ckr::DevBuf<uint32_t> tri_light;
   ckr::DevBuf<float> pcdf, sel_cdf;
@@ -106,4 +107,6 @@ namespace ckr {
 SceneView view_of(const ckr_scene *s);
 uint32_t stack_depth_of(const ckr_scene *s);
 ShadeView shade_view_of(const ckr_scene *s);
+// Fills s->tri_nm from the uploaded vertices and materials (synchronous).
+int build_tri_nm(ckr_scene *s);
 }  // namespace ckr

@@ -15,6 +15,7 @@ ShadeView shade_view_of(const ckr_scene *s) {
   v.mats = s->mats.ptr;
   v.tri_mat = s->tri_mat.ptr;
   v.tri9 = s->tri9.ptr;
+  v.tri_nm = s->tri_nm.ptr;
   v.sph_mat = s->sph_mat.ptr;
   v.sph = s->spheres.ptr;
   v.lights = s->lights.ptr;
@@ -252,6 +253,10 @@ extern "C" int ckr_scene_create_ex(const ckr_scene_desc *d, ckr_scene **out) {
       (st = upload(s->env_marg, env.marg.data(), env.marg.size())) != CKR_OK ||
       (st = upload(s->env_cond, env.cond.data(), env.cond.size())) != CKR_OK ||
       (st = upload(s->env_cos, env.cosr.data(), env.cosr.size())) != CKR_OK) {
+    ckr_scene_destroy(s);
+    return st;
+  }
+  if ((st = build_tri_nm(s)) != CKR_OK) {
     ckr_scene_destroy(s);
     return st;
   }

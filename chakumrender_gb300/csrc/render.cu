@@ -1,13 +1,15 @@
 // render.cu — wavefront renderer: camera rays -> closest hit -> shade (MIS light
 // sampling, BRDF-sampled continuation) -> shadow rays -> FP64 accumulation.
 //
-// Paths are processed in waves of up to `wave` paths.  Each bounce runs three
-// persistent kernels over device-side queues: k_extend (closest hit),
-// k_shade (emits shadow rays and the continuation ray into queues whose slots
-// are reserved once per warp: a warp-wide prefix sum of the per-lane counts and
-// one atomicAdd by lane 0), k_shadow (any hit, adds unoccluded contributions).
-// Queue lengths live in device memory, so a whole render is a fixed sequence of
-// launches with no host synchronisation (capturable in a CUDA graph).
+// Paths live in up to `wave` path slots.  Each step runs three persistent kernels
+// over device-side queues: k_extend (closest hit), k_shade (emits shadow rays and
+// the continuation ray into queues whose slots are reserved once per warp: a
+// warp-wide prefix sum of the per-lane counts and one atomicAdd by lane 31),
+// k_shadow (any hit, adds unoccluded contributions).  Path tracers of more than
+// one wave regenerate: a path that ends hands its slot to the next camera path,
+// and the host stops on an empty queue.  Otherwise (direct-light shaders, single
+// waves, inside stream capture) paths run in waves of one step per bounce, a
+// fixed launch sequence with no host synchronisation (capturable in a CUDA graph).
 //
 // Shaders (ckr_render_cfg.shader):
 //   DIRECT_MISCV  shadeDirectOnly + getLightFromMeshSource_Analytic_MISCV

@@ -270,11 +270,15 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   // shading step that ends a path starts the next camera path in its slot, so
   // every step runs a full queue until the last paths have started.  The host
   // stops when the queue is empty, reading its length one step behind so that the
-  // device always has the next step queued.
+  // device always has the next step queued.  It pays where traversal is long
+  // (trees of kDynamicDepth levels or more: many-light frame 0.364 -> 0.312 s);
+  // on shallow trees a step is short and mixing camera rays with bounce rays in
+  // one queue costs more than the drained waves' tails (box, 1024^2 x 64 spp:
+  // 111 ms against 98 ms with waves), so those keep the waves.
   cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
   CKR_CUDA_TRY(cudaStreamIsCapturing(stream, &capture));
   const bool regen = (cfg->shader == CKR_SHADER_PATH || cfg->shader == CKR_SHADER_PATH_NEE) && total > wave &&
-                     capture == cudaStreamCaptureStatusNone && total + 64ull * wave < (1ull << 32);
+                     dyn && capture == cudaStreamCaptureStatusNone && total + 64ull * wave < (1ull << 32);
   if (regen) {
     if (!W.h_count) CKR_CUDA_TRY(cudaMallocHost((void **)&W.h_count, 2 * sizeof(uint32_t)));
     for (cudaEvent_t &e : W.ev)

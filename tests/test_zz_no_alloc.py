@@ -47,14 +47,16 @@ def test_noalloc_matches_render(torch_cuda, shader, spp, nl, nb, depth):
 
 @pytest.mark.parametrize("shader", [S.SHADER_PATH, S.SHADER_PATH_NEE])
 def test_regenerating_render_matches_waves(torch_cuda, shader):
-    """A path-tracer render of more than one wave of paths (here 4,194,304 against 2^21
-    slots) starts a new camera path in the slot of every path that ends; the same paths
-    rendered in fixed waves of 32,768 (ckr_render_noalloc) give the same image."""
-    sd = S.load_xml(S.SCENES / "box.xml")
+    """A path-tracer render of more than one wave of paths on a tree of three or more
+    levels (here 4,194,304 paths against 2^21 slots, a 5,120-triangle icosphere in the
+    many-light room with 64 emitters in 4 clusters) starts a new camera path in the slot
+    of every path that ends; the same paths rendered in fixed waves of 32,768
+    (ckr_render_noalloc) give the same image."""
+    sd = S.manylight_scene(S.manylight_spec(subdiv=4, width=512, height=512, nemit=64, nclusters=4))
     cam = sd.camera
-    cam.width = cam.height = 512
     cfg = S.render_cfg(shader=shader, spp=16, n_light=1, n_brdf=1, max_depth=5)
     scene = S.RenderScene(sd)
+    assert scene.info().max_depth >= 3  # deep enough for regeneration
     ref = scene.render_host(cam, cfg)
     st, img = noalloc(scene, cam, cfg, torch_cuda)
     assert st == 0

@@ -2,12 +2,13 @@
 // src/lightSources_CV.cpp:323-333, per pixel).
 //
 // The kernel is FP32-ALU bound (per pixel and emitter triangle: three
-// transformed vertices, horizon clipping, 3-4 edge integrals with acos/sin,
-// for both the specular LTC lobe and the diffuse cosine lobe).  The 64x64 LTC
-// table (Minv's five non-zeros + amplitude, 96 KB) is staged once per CTA into
-// shared memory; CTAs are persistent (one or two per SM) and stride over pixels.
-// Emitter triangles are read through the read-only path (every thread of a warp
-// reads the same triangle, a broadcast).
+// transformed vertices, horizon clipping, 3-4 edge integrals, for both the
+// specular LTC lobe and the diffuse cosine lobe) and its lanes disagree on the
+// path a triangle takes (above, below or across the horizon), so triangles across
+// the horizon are queued per warp and clipped by all lanes together (k_ltc_shade).
+// CTAs are persistent (two per SM) and stride over pixels; the 64x64 LTC table is
+// read from global memory (two entries per pixel), emitter triangles through the
+// read-only path (every lane of a warp reads the same triangle, a broadcast).
 #include <algorithm>
 
 #include "ckr_internal.h"
@@ -18,35 +19,47 @@
 namespace ckr {
 namespace {
 
-constexpr int kLtcTPB = 256;
+constexpr int kLtcTPB = 256, kLtcWarps = kLtcTPB / 32;
+constexpr uint32_t kLtcQueue = 512;  // deferred triangles per warp and batch of 32 pixels
 
-struct SmemTable {
-  const float4 *a;  // mi0 mi2 mi4 mi6
-  const float2 *b;  // mi8 amp
-  SHD LtcEntry operator()(int i) const {
-    float4 x = a[i];
-    float2 y = b[i];
-    LtcEntry e;
-    e.mi0 = x.x; e.mi2 = x.y; e.mi4 = x.z; e.mi6 = x.w; e.mi8 = y.x; e.amp = y.y;
-    e.m0 = e.m2 = e.m4 = e.m6 = e.m8 = e.det = 0.f;
-    return e;
-  }
+// The clipped integrals for a lane whose warp's queue is full.  Out of line: inlined
+// into the classifying loop they pushed it past 128 registers (60 bytes of spills,
+// 1.20 ms per 1024^2 frame against 0.84 ms).
+__device__ __noinline__ float clipped_diffuse_here(F3 A, F3 B, F3 C, F3 n, F3 x) {
+  return ltc_diffuse_clipped(A, B, C, n, x);
+}
+__device__ __noinline__ float clipped_spec_here(F3 A, F3 B, F3 C, F3 x, M3f m) {
+  return ltc_spec_clipped(A, B, C, x, m);
+}
+
+// LTC table entries straight from global memory: two per pixel, through L1.
+struct GlobalTable {
+  const LtcEntry *t;
+  SHD LtcEntry operator()(int i) const { return t[i]; }
 };
 
+// Per warp: its 32 pixels' shading frames and the emitter triangles it deferred.
+struct LtcWarp {
+  float px[32][17];          // x (3), n (3), Minv in world space (9); padded against bank conflicts
+  float res[kLtcQueue][3];   // a deferred triangle's contribution, colour-weighted
+  uint2 item[kLtcQueue];     // (lane | lobe << 5 | light << 6, previous item of the same lane or ~0)
+};
+
+// getLightFromMeshSource_Analytic per pixel, one pixel per lane.  Per emitter
+// triangle and lobe a lane settles the triangles wholly above or below its horizon
+// at once; a triangle across the horizon (clipping, four edge integrals) is queued,
+// and the warp then works through its queue with every lane busy instead of letting
+// the few lanes that clip hold up the rest.  Each lane adds its queued terms in a
+// fixed order (newest first), so the result does not depend on scheduling.  A full
+// queue falls back to clipping in place.
 __global__ void __launch_bounds__(kLtcTPB, 2) k_ltc_shade(const float4 *__restrict__ gbuf, uint32_t npx,
                                                        const float *__restrict__ light_tri9,
                                                        const float *__restrict__ light_rgb, uint32_t nlight,
                                                        float *__restrict__ rgb, const LtcEntry *__restrict__ table) {
-  extern __shared__ float4 smem[];
-  float4 *sa = smem;
-  float2 *sb = reinterpret_cast<float2 *>(smem + 4096);
-  for (int i = threadIdx.x; i < 4096; i += kLtcTPB) {
-    const LtcEntry &e = table[i];
-    sa[i] = make_float4(e.mi0, e.mi2, e.mi4, e.mi6);
-    sb[i] = make_float2(e.mi8, e.amp);
-  }
-  __syncthreads();
-  SmemTable tab{sa, sb};
+  extern __shared__ __align__(16) unsigned char ltc_smem[];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  LtcWarp &W = reinterpret_cast<LtcWarp *>(ltc_smem)[warp];
+  const GlobalTable tab{table};
   auto light = [&](uint32_t k, F3 &A, F3 &B, F3 &C, float *c) {
     const float *t = light_tri9 + 9 * (size_t)k;
     A = f3(__ldg(t), __ldg(t + 1), __ldg(t + 2));
@@ -56,14 +69,95 @@ __global__ void __launch_bounds__(kLtcTPB, 2) k_ltc_shade(const float4 *__restri
     c[1] = __ldg(light_rgb + 3 * k + 1);
     c[2] = __ldg(light_rgb + 3 * k + 2);
   };
-  for (uint32_t p = blockIdx.x * kLtcTPB + threadIdx.x; p < npx; p += gridDim.x * kLtcTPB) {
-    float4 g0 = gbuf[3 * (size_t)p], g1 = gbuf[3 * (size_t)p + 1], g2 = gbuf[3 * (size_t)p + 2];
-    float out[3];
-    ltc_shade_point(tab, f3(g0.x, g0.y, g0.z), f3(g1.x, g1.y, g1.z), f3(g2.x, g2.y, g2.z), g0.w, g2.w, nlight,
-                    light, out);
-    rgb[3 * (size_t)p] = out[0];
-    rgb[3 * (size_t)p + 1] = out[1];
-    rgb[3 * (size_t)p + 2] = out[2];
+  const float inv2pi = 1.0f / (2.0f * kPi);
+  for (uint32_t base = (blockIdx.x * kLtcWarps + warp) * 32u; base < npx; base += gridDim.x * (uint32_t)kLtcTPB) {
+    const uint32_t p = base + lane;
+    const bool active = p < npx;
+    F3 x = f3(0, 0, 0), n = f3(0, 0, 1);
+    M3f minv{};
+    float amp = 0.f, spec = 0.f;
+    if (active) {
+      const float4 g0 = gbuf[3 * (size_t)p], g1 = gbuf[3 * (size_t)p + 1], g2 = gbuf[3 * (size_t)p + 2];
+      x = f3(g0.x, g0.y, g0.z);
+      n = f3(g1.x, g1.y, g1.z);
+      const F3 wo = f3(g2.x, g2.y, g2.z);
+      const float theta = acosf(fminf(1.0f, fmaxf(-1.0f, dot(n, wo))));
+      const LtcLookup L = ltc_lookup(tab, theta, g0.w);
+      minv = ltc_minv_world(L, n, wo);
+      amp = L.amp;
+      spec = g2.w;
+    }
+    float *mine = W.px[lane];
+    mine[0] = x.x; mine[1] = x.y; mine[2] = x.z;
+    mine[3] = n.x; mine[4] = n.y; mine[5] = n.z;
+    for (int i = 0; i < 9; ++i) mine[6 + i] = minv.a[i];
+    float s3[3] = {0.f, 0.f, 0.f}, d3[3] = {0.f, 0.f, 0.f};
+    uint32_t head = ~0u, count = 0;  // count: the same in every lane
+    for (uint32_t k = 0; k < nlight; ++k) {
+      F3 A, B, C;
+      float c[3];
+      light(k, A, B, C, c);
+      float s = 0.f, d = 0.f;
+      int cs = 0, cd = 0;
+      if (active) {
+        cs = ltc_spec_case(A, B, C, x, minv, s);
+        cd = ltc_diffuse_case(A, B, C, n, x, d);
+      }
+      for (int j = 0; j < 3; ++j) {
+        s3[j] += c[j] * s;
+        d3[j] += c[j] * d;
+      }
+      for (uint32_t lobe = 0; lobe < 2; ++lobe) {
+        const bool want = (lobe ? cd : cs) < 0;
+        const unsigned m = __ballot_sync(0xffffffffu, want);
+        const uint32_t slot = count + (uint32_t)__popc(m & ((1u << lane) - 1u));
+        if (want) {
+          if (slot < kLtcQueue) {
+            W.item[slot] = make_uint2(lane | lobe << 5 | k << 6, head);
+            head = slot;
+          } else if (lobe) {
+            const float v = clipped_diffuse_here(A, B, C, n, x);
+            for (int j = 0; j < 3; ++j) d3[j] += c[j] * v;
+          } else {
+            const float v = clipped_spec_here(A, B, C, x, minv);
+            for (int j = 0; j < 3; ++j) s3[j] += c[j] * v;
+          }
+        }
+        count += (uint32_t)__popc(m);
+      }
+    }
+    __syncwarp();
+    // The warp's queued triangles, every lane taking the next one.
+    const uint32_t nq = count < kLtcQueue ? count : kLtcQueue;
+    for (uint32_t i = lane; i < nq; i += 32) {
+      const uint2 it = W.item[i];
+      const uint32_t pl = it.x & 31u, k = it.x >> 6;
+      const float *q = W.px[pl];
+      F3 A, B, C;
+      float c[3];
+      light(k, A, B, C, c);
+      const F3 qx = f3(q[0], q[1], q[2]);
+      float v;
+      if ((it.x >> 5) & 1u) {
+        v = ltc_diffuse_clipped(A, B, C, f3(q[3], q[4], q[5]), qx);
+      } else {
+        M3f qm;
+        for (int j = 0; j < 9; ++j) qm.a[j] = q[6 + j];
+        v = ltc_spec_clipped(A, B, C, qx, qm);
+      }
+      for (int j = 0; j < 3; ++j) W.res[i][j] = c[j] * v;
+    }
+    __syncwarp();
+    for (uint32_t i = head; i != ~0u; i = W.item[i].y) {
+      if ((W.item[i].x >> 5) & 1u) {
+        for (int j = 0; j < 3; ++j) d3[j] += W.res[i][j];
+      } else {
+        for (int j = 0; j < 3; ++j) s3[j] += W.res[i][j];
+      }
+    }
+    if (active)
+      for (int j = 0; j < 3; ++j) rgb[3 * (size_t)p + j] = s3[j] * inv2pi * amp * spec + d3[j] * inv2pi * (1.0f - spec);
+    __syncwarp();  // the next batch reuses the warp's shared memory
   }
 }
 
@@ -197,7 +291,8 @@ extern "C" int ckr_ltc_shade(const float *gbuf, uint32_t npx, const float *light
   int st = CKR_OK;
   const LtcEntry *table = device_ltc_table(&st);
   if (!table) return st;
-  const size_t smem = 4096 * (sizeof(float4) + sizeof(float2));
+  if (nlight >= (1u << 26)) return CKR_ERR_TOO_LARGE;  // light index in a queue item
+  const size_t smem = kLtcWarps * sizeof(LtcWarp);
   static bool attr_set[64] = {false};
   int dev = 0, sms = 0, per_sm = 0;
   CKR_CUDA_TRY(cudaGetDevice(&dev));

@@ -475,47 +475,68 @@ SHD bool clip_triangle_z(F3 A, F3 B, F3 C, float nA, float nB, float nC, Clip4 &
 }
 
 // |polygon integral| of one emitter triangle for the cosine lobe about n at x
-// (getLightAnalyticDiffuse inner loop, src/lightSources_CV.cpp:226-264).
-SHD float ltc_diffuse_tri(F3 A, F3 B, F3 C, F3 n, F3 x) {
+// (getLightAnalyticDiffuse inner loop, src/lightSources_CV.cpp:226-264), in two
+// parts: ltc_diffuse_case settles a triangle wholly above (1, |integral| in d) or
+// below (0, d = 0) the horizon and returns -1 for one across it, whose clipped
+// integral is ltc_diffuse_clipped.
+SHD int ltc_diffuse_case(F3 A, F3 B, F3 C, F3 n, F3 x, float &d) {
   F3 e1 = normalize(A - x), e2 = normalize(B - x), e3 = normalize(C - x);
   float nA = dot(e1, n), nB = dot(e2, n), nC = dot(e3, n);
-  float sum;
+  d = 0.0f;
   if (nA > 0.f && nB > 0.f && nC > 0.f) {
-    sum = integrate_edge(e1, e2, n) + integrate_edge(e2, e3, n) + integrate_edge(e3, e1, n);
-  } else if (nA < 0.f && nB < 0.f && nC < 0.f) {
-    return 0.0f;
-  } else {
-    Clip4 clip;
-    clip.q0 = clip.q1 = clip.q2 = clip.q3 = f3(0, 0, 0);
-    if (!clip_triangle(A, B, C, n, x, nA, nB, nC, clip)) return 0.0f;
-    F3 c0 = normalize(clip.q0 - x), c1 = normalize(clip.q1 - x), c2 = normalize(clip.q2 - x),
-       c3 = normalize(clip.q3 - x);
-    sum = integrate_edge(c0, c1, n) + integrate_edge(c1, c2, n) + integrate_edge(c2, c3, n) +
-          integrate_edge(c3, c0, n);
+    d = fabsf(integrate_edge(e1, e2, n) + integrate_edge(e2, e3, n) + integrate_edge(e3, e1, n));
+    return 1;
   }
-  return fabsf(sum);
+  if (nA < 0.f && nB < 0.f && nC < 0.f) return 0;
+  return -1;
+}
+
+SHD float ltc_diffuse_clipped(F3 A, F3 B, F3 C, F3 n, F3 x) {
+  F3 e1 = normalize(A - x), e2 = normalize(B - x), e3 = normalize(C - x);
+  float nA = dot(e1, n), nB = dot(e2, n), nC = dot(e3, n);
+  Clip4 clip;
+  clip.q0 = clip.q1 = clip.q2 = clip.q3 = f3(0, 0, 0);
+  if (!clip_triangle(A, B, C, n, x, nA, nB, nC, clip)) return 0.0f;
+  F3 c0 = normalize(clip.q0 - x), c1 = normalize(clip.q1 - x), c2 = normalize(clip.q2 - x),
+     c3 = normalize(clip.q3 - x);
+  return fabsf(integrate_edge(c0, c1, n) + integrate_edge(c1, c2, n) + integrate_edge(c2, c3, n) +
+               integrate_edge(c3, c0, n));
+}
+
+SHD float ltc_diffuse_tri(F3 A, F3 B, F3 C, F3 n, F3 x) {
+  float d;
+  return ltc_diffuse_case(A, B, C, n, x, d) < 0 ? ltc_diffuse_clipped(A, B, C, n, x) : d;
 }
 
 // |polygon integral| of one emitter triangle in the LTC's canonical space
-// (getLightAnalytic inner loop, src/lightSources_CV.cpp:278-317).
-SHD float ltc_spec_tri(F3 A, F3 B, F3 C, F3 x, const M3f &minv) {
+// (getLightAnalytic inner loop, src/lightSources_CV.cpp:278-317), split the same way.
+SHD int ltc_spec_case(F3 A, F3 B, F3 C, F3 x, const M3f &minv, float &s) {
   F3 e1 = mul(minv, A - x), e2 = mul(minv, B - x), e3 = mul(minv, C - x);
-  float sum;
+  s = 0.0f;
   if (e1.z > 0.f && e2.z > 0.f && e3.z > 0.f) {
     e1 = normalize(e1);
     e2 = normalize(e2);
     e3 = normalize(e3);
-    sum = integrate_edge_z(e1, e2) + integrate_edge_z(e2, e3) + integrate_edge_z(e3, e1);
-  } else if (e1.z < 0.f && e2.z < 0.f && e3.z < 0.f) {
-    return 0.0f;
-  } else {
-    Clip4 clip;
-    clip.q0 = clip.q1 = clip.q2 = clip.q3 = f3(0, 0, 0);
-    if (!clip_triangle_z(e1, e2, e3, e1.z / length(e1), e2.z / length(e2), e3.z / length(e3), clip)) return 0.0f;
-    F3 c0 = normalize(clip.q0), c1 = normalize(clip.q1), c2 = normalize(clip.q2), c3 = normalize(clip.q3);
-    sum = integrate_edge_z(c0, c1) + integrate_edge_z(c1, c2) + integrate_edge_z(c2, c3) + integrate_edge_z(c3, c0);
+    s = fabsf(integrate_edge_z(e1, e2) + integrate_edge_z(e2, e3) + integrate_edge_z(e3, e1));
+    return 1;
   }
-  return fabsf(sum);
+  if (e1.z < 0.f && e2.z < 0.f && e3.z < 0.f) return 0;
+  return -1;
+}
+
+SHD float ltc_spec_clipped(F3 A, F3 B, F3 C, F3 x, const M3f &minv) {
+  F3 e1 = mul(minv, A - x), e2 = mul(minv, B - x), e3 = mul(minv, C - x);
+  Clip4 clip;
+  clip.q0 = clip.q1 = clip.q2 = clip.q3 = f3(0, 0, 0);
+  if (!clip_triangle_z(e1, e2, e3, e1.z / length(e1), e2.z / length(e2), e3.z / length(e3), clip)) return 0.0f;
+  F3 c0 = normalize(clip.q0), c1 = normalize(clip.q1), c2 = normalize(clip.q2), c3 = normalize(clip.q3);
+  return fabsf(integrate_edge_z(c0, c1) + integrate_edge_z(c1, c2) + integrate_edge_z(c2, c3) +
+               integrate_edge_z(c3, c0));
+}
+
+SHD float ltc_spec_tri(F3 A, F3 B, F3 C, F3 x, const M3f &minv) {
+  float s;
+  return ltc_spec_case(A, B, C, x, minv, s) < 0 ? ltc_spec_clipped(A, B, C, x, minv) : s;
 }
 
 // getLightFromMeshSource_Analytic for one shading point (src/lightSources_CV.cpp:323-333):

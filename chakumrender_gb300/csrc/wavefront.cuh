@@ -1,14 +1,16 @@
 // wavefront.cuh — the renderer's wavefront kernels (device code shared by the
 // single-render entry points, render.cu, and the batched renderer, batch.cu).
 //
-// A render is processed in waves of paths.  Each bounce runs three persistent
-// kernels over device-side queues: k_extend (closest hit), k_shade (emits
-// shadow rays and the continuation ray into queues whose slots are reserved once
-// per warp: a warp-wide prefix sum of the per-lane counts and one atomicAdd by
-// lane 0), k_shadow (any hit, adds unoccluded contributions).  Queue lengths live
-// in device memory, so a whole render is a fixed sequence of launches with no host
-// synchronisation (capturable in a CUDA graph).  Kernels are templated on the
-// block size (the traversal stack in shared memory is laid out [level][thread]).
+// Paths occupy path slots.  Each step runs three persistent kernels over
+// device-side queues: k_extend (closest hit), k_shade (emits shadow rays and the
+// continuation ray into queues whose slots are reserved once per warp: a
+// warp-wide prefix sum of the per-lane counts and one atomicAdd by lane 31),
+// k_shadow (any hit, adds unoccluded contributions).  Queue lengths live in device
+// memory.  Paths run in waves (a fixed sequence of launches with no host
+// synchronisation, capturable in a CUDA graph), or, with Params::regen_total set,
+// a shading step that ends a path starts the next camera path in its slot
+// (regenerate).  Kernels are templated on the block size (the traversal stack in
+// shared memory is laid out [level][thread]).
 //
 // Batches: with Params::jobs set, a path carries its job index in meta.w >> 8 and
 // the job supplies the camera, the material table offset, the random seed, the

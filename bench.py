@@ -521,8 +521,26 @@ def case_ltc():
     torch.cuda.synchronize()
 
 
+def case_ltc_mc():
+    """The Monte Carlo reference of the LTC integral on 65,536 pixels of the same
+    G-buffer, 4,096 samples per pixel, once, for profilers."""
+    import torch
+    from chakumrender_gb300 import build
+    from chakumrender_gb300 import ckr
+
+    build.build_library()
+    n = 65536
+    g = torch.from_numpy(ckr.gbuffer(2, n)).cuda()
+    lt, lc = ckr.quad_lights(3, 8)
+    dt, dc = torch.from_numpy(lt).cuda(), torch.from_numpy(lc).cuda()
+    out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    ckr.ltc_mc(g.data_ptr(), n, dt.data_ptr(), dc.data_ptr(), len(lt), 4096, 9, 0, out.data_ptr(),
+               torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+
+
 CASES = {"manylight-learned": case_manylight_learned, "manylight-split": case_manylight_split, "trace": case_trace,
-         "ltc": case_ltc}
+         "ltc": case_ltc, "ltc-mc": case_ltc_mc}
 
 
 def main():

@@ -706,9 +706,12 @@ __global__ void __launch_bounds__(TPB, (512 / TPB > 1 ? 512 / TPB : 1))
 // distribution, one of its triangles in proportion to power and a uniform point
 // on it; the BRDF sample continues the path and, if it meets an emitter, is
 // weighted at the next vertex with the light technique's pdf of the previous
-// vertex (its pdf is carried in beta.w).  Balance heuristic throughout.
+// vertex (its pdf is carried in beta.w).  Balance heuristic throughout.  Launched
+// with 1024 / TPB resident blocks (64 registers at 128 threads, some spills): the
+// many-light frame at 640 / 768 / 896 / 1024 was 0.3135 / 0.3110 / 0.3042 /
+// 0.3040 s, the extra resident warps hiding the vertex's dependent loads.
 template <int TPB>
-__global__ void __launch_bounds__(TPB, (640 / TPB > 1 ? 640 / TPB : 1))
+__global__ void __launch_bounds__(TPB, (1024 / TPB > 1 ? 1024 / TPB : 1))
     k_shade_nee(ShadeView sv0, Paths P, Params prm, int cur, Learn lr) {
   const uint32_t n = P.counts[cur];
   const uint32_t *q = cur ? P.q1 : P.q0;

@@ -693,10 +693,12 @@ __global__ void __launch_bounds__(TPB, (640 / TPB > 1 ? 640 / TPB : 1))
   shade<CKR_SHADER_PATH, TPB>(sv0, P, prm, cur, depth, ltc, SceneView{}, 0);
 }
 
-// The reference's default shader (MISCV) at 512 / TPB resident blocks (128
-// registers at 128 threads): at 154 spill-free registers it was 8 % slower.
+// The reference's default shader (MISCV) at 1024 / TPB resident blocks (64
+// registers at 128 threads, with spills): box, 512^2 x 4 spp, 10 light + 60 BRDF
+// samples: 6.13 ms at 512 / TPB (128 registers), 6.24 at 640, 5.89 at 768, 5.51 at
+// 1024, 5.83 at 1280, 5.78 at 1536; at 154 spill-free registers it was slower still.
 template <int TPB>
-__global__ void __launch_bounds__(TPB, (512 / TPB > 1 ? 512 / TPB : 1))
+__global__ void __launch_bounds__(TPB, (1024 / TPB > 1 ? 1024 / TPB : 1))
     k_shade_miscv(ShadeView sv0, Paths P, Params prm, int cur, int depth, const LtcEntry *__restrict__ ltc) {
   shade<CKR_SHADER_DIRECT_MISCV, TPB>(sv0, P, prm, cur, depth, ltc, SceneView{}, 0);
 }

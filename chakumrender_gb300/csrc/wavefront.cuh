@@ -679,9 +679,16 @@ __device__ __forceinline__ void shade(ShadeView sv0, Paths P, Params prm, int cu
 // Shading kernels.  The MIS path tracer's vertex is register hungry but short: at
 // 640 / TPB resident blocks (96 registers at 128 threads, with some spills) the box
 // frame took 1.50 ms against 1.65 ms at the default 149 registers.  The direct-light
-// shaders keep the compiler's choice, except MISCV (k_shade_miscv below).
+// shaders run at 1024 / TPB resident blocks (64 registers at 128 threads): box
+// 512^2 x 4 spp, 10 light + 60 BRDF samples, DIRECT_MIS 10.0 -> 7.8 ms, DIRECT_CV
+// 2.46 -> 2.40 ms against the compiler's choice; the explicit path loop, which
+// traverses inside the kernel, keeps the compiler's choice.
+constexpr int shade_blocks(uint32_t shader, int tpb) {
+  return shader == CKR_SHADER_EXPLICIT || 1024 / tpb < 1 ? 1 : 1024 / tpb;
+}
+
 template <uint32_t SHADER, int TPB>
-__global__ void __launch_bounds__(TPB) k_shade(ShadeView sv0, Paths P, Params prm, int cur, int depth,
+__global__ void __launch_bounds__(TPB, shade_blocks(SHADER, TPB)) k_shade(ShadeView sv0, Paths P, Params prm, int cur, int depth,
                                                  const LtcEntry *__restrict__ ltc, SceneView scene = SceneView{},
                                                  int stack_depth = 0) {
   shade<SHADER, TPB>(sv0, P, prm, cur, depth, ltc, scene, stack_depth);

@@ -681,10 +681,11 @@ __device__ __forceinline__ void shade(ShadeView sv0, Paths P, Params prm, int cu
 // frame took 1.50 ms against 1.65 ms at the default 149 registers.  The direct-light
 // shaders run at 1024 / TPB resident blocks (64 registers at 128 threads): box
 // 512^2 x 4 spp, 10 light + 60 BRDF samples, DIRECT_MIS 10.0 -> 7.8 ms, DIRECT_CV
-// 2.46 -> 2.40 ms against the compiler's choice; the explicit path loop, which
-// traverses inside the kernel, keeps the compiler's choice.
+// 2.46 -> 2.40 ms against the compiler's choice.  The explicit path loop, which
+// traverses inside the kernel, at 512 / TPB (128 registers; box 256^2 x 4 spp,
+// depth 4: 7.01 ms at the compiler's 195 registers, 4.81 ms, 5.06 ms at 640 / TPB).
 constexpr int shade_blocks(uint32_t shader, int tpb) {
-  return shader == CKR_SHADER_EXPLICIT || 1024 / tpb < 1 ? 1 : 1024 / tpb;
+  return shader == CKR_SHADER_EXPLICIT ? (512 / tpb > 1 ? 512 / tpb : 1) : (1024 / tpb > 1 ? 1024 / tpb : 1);
 }
 
 template <uint32_t SHADER, int TPB>

@@ -539,8 +539,26 @@ def case_ltc_mc():
     torch.cuda.synchronize()
 
 
+def case_box():
+    """The box render of the benchmark (256x256, 16 spp, depth 4, MIS 1 + 1), three
+    frames, for profilers."""
+    import torch
+    from chakumrender_gb300 import build
+    from chakumrender_gb300 import scene as S
+
+    build.build_library()
+    sd = S.load_xml(S.SCENES / "box.xml")
+    cam = sd.camera
+    cfg = S.render_cfg(shader=S.SHADER_PATH, spp=16, max_depth=4, n_light=1, n_brdf=1, rr_prob=0.3, seed=1)
+    scene = S.RenderScene(sd)
+    rgb = torch.empty((cam.height, cam.width, 3), dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        scene.render(cam, cfg, rgb.data_ptr())
+    torch.cuda.synchronize()
+
+
 CASES = {"manylight-learned": case_manylight_learned, "manylight-split": case_manylight_split, "trace": case_trace,
-         "ltc": case_ltc, "ltc-mc": case_ltc_mc}
+         "ltc": case_ltc, "ltc-mc": case_ltc_mc, "box": case_box}
 
 
 def main():

@@ -125,6 +125,19 @@ __device__ __forceinline__ bool hit_triangle(const RayPre &r, float4 v0, float4 
 // Sphere::intersect in FP64 (src/geometryPrimitives.cpp:12-27), with the
 // root taken above max(tmin, 1e-4).
 __device__ __forceinline__ double hit_sphere(const RayPre &r, float4 s) {
+  {
+    // FP32 pre-test (FP64 is slow on this part): a ray whose line passes the sphere
+    // by more than 1e-5 of the squared magnitudes involved -- orders of magnitude
+    // above the FP32 rounding of these few operations -- has a negative FP64
+    // discriminant too, so the miss is decided without FP64.  NaN and overflow fall
+    // through to the FP64 test.
+    const float ox = s.x - r.ox, oy = s.y - r.oy, oz = s.z - r.oz;
+    const float b = ox * r.dx + oy * r.dy + oz * r.dz;
+    const float oo = ox * ox + oy * oy + oz * oz;
+    const float m = fmaxf(fmaxf(fmaxf(fabsf(s.x), fabsf(s.y)), fabsf(s.z)),
+                          fmaxf(fmaxf(fabsf(r.ox), fabsf(r.oy)), fabsf(r.oz)));
+    if (b * b - oo + s.w * s.w < -1e-5f * (m * m + oo + b * b + s.w * s.w)) return 1e300;
+  }
   double opx = (double)s.x - r.ox, opy = (double)s.y - r.oy, opz = (double)s.z - r.oz;
   double dx = r.dx, dy = r.dy, dz = r.dz;
   double b = opx * dx + opy * dy + opz * dz;

@@ -101,6 +101,7 @@ struct ckr_scene {
   cudaStream_t pipe[kMaxPipes] = {};
   cudaEvent_t pipe_done[kMaxPipes] = {};
   cudaEvent_t user_ready = nullptr;
+  int *h_status = nullptr;  // pinned: the status word read back at the end of a host-buffer query
 };
 
 namespace ckr {

@@ -188,6 +188,7 @@ extern "C" int ckr_scene_destroy(ckr_scene *scene) {
   for (auto &e : scene->pipe_done)
     if (e) cudaEventDestroy(e);
   if (scene->user_ready) cudaEventDestroy(scene->user_ready);
+  if (scene->h_status) cudaFreeHost(scene->h_status);
   if (scene->render_ws && scene->render_ws_free) scene->render_ws_free(scene->render_ws);
   delete scene;
   return CKR_OK;
@@ -317,9 +318,12 @@ int trace_host(ckr_scene *s, const ckr_ray *rays, uint32_t n, uint32_t *hit_id, 
     CKR_CUDA_TRY(cudaEventRecord(s->pipe_done[k], s->pipe[k]));
     CKR_CUDA_TRY(cudaStreamWaitEvent(user, s->pipe_done[k], 0));
   }
+  // The status word comes back in the same stream order, so one synchronisation
+  // covers the traversal, the results and the status.
+  if (!s->h_status) CKR_CUDA_TRY(cudaMallocHost((void **)&s->h_status, sizeof(int)));
+  CKR_CUDA_TRY(cudaMemcpyAsync(s->h_status, s->status.ptr, sizeof(int), cudaMemcpyDeviceToHost, user));
   CKR_CUDA_TRY(cudaStreamSynchronize(user));
-  int h = 0;
-  CKR_CUDA_TRY(cudaMemcpy(&h, s->status.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+  const int h = *s->h_status;
   if (h != 0) {
     CKR_CUDA_TRY(cudaMemset(s->status.ptr, 0, sizeof(int)));
     return h;

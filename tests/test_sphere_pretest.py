@@ -1,0 +1,63 @@
+"""The FP32 pre-test in front of the FP64 sphere test (hit_sphere, csrc/trace_device.cuh)
+may only settle misses: wherever it reports a miss, the FP64 discriminant the reference's
+Sphere::intersect computes (src/geometryPrimitives.cpp:12-27) must be negative too.  The
+predicate is restated here in float32 and checked against float64 on random, grazing and
+large-sphere cases.  No GPU."""
+from __future__ import annotations
+
+import numpy as np
+
+F = np.float32
+
+
+def pretest_miss(c, r, o, d):
+    """The device predicate, float32 throughout (the device may fuse multiply-adds,
+    which only rounds less)."""
+    ox, oy, oz = (c[:, 0] - o[:, 0]), (c[:, 1] - o[:, 1]), (c[:, 2] - o[:, 2])
+    b = ox * d[:, 0] + oy * d[:, 1] + oz * d[:, 2]
+    oo = ox * ox + oy * oy + oz * oz
+    m = np.maximum(np.abs(c).max(1), np.abs(o).max(1))
+    return b * b - oo + r * r < F(-1e-5) * (m * m + oo + b * b + r * r)
+
+
+def fp64_det(c, r, o, d):
+    op = c.astype(np.float64) - o.astype(np.float64)
+    b = (op * d.astype(np.float64)).sum(1)
+    return b * b - (op * op).sum(1) + r.astype(np.float64) ** 2
+
+
+def unit(v):
+    return (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(F)
+
+
+def test_pretest_never_rejects_a_hit():
+    rng = np.random.default_rng(4)
+    n = 400000
+    cases = []
+    # Small spheres near the origin (the box scene), rays from anywhere nearby.
+    c = rng.uniform(-1, 1, (n, 3)).astype(F)
+    r = rng.uniform(0.01, 0.5, n).astype(F)
+    o = rng.uniform(-2, 2, (n, 3)).astype(F)
+    cases.append((c, r, o, unit(rng.normal(size=(n, 3)))))
+    # Grazing rays: aimed at a point on the silhouette, perturbed by 1e-7 .. 1e-3.
+    d = unit(rng.normal(size=(n, 3)))
+    side = unit(np.cross(d, rng.normal(size=(n, 3))))
+    eps = 10 ** rng.uniform(-7, -3, n)
+    target = c + side * (r * (1 + rng.choice([-1, 1], n) * eps))[:, None]
+    o2 = (target - d * rng.uniform(0.5, 3, n)[:, None]).astype(F)
+    cases.append((c, r, o2, unit(target - o2)))
+    # The reference's 1e5-radius walls and far-off scenes.
+    cw = (rng.normal(size=(n, 3)) * 1e5).astype(F)
+    rw = (np.linalg.norm(cw, axis=1) * rng.uniform(0.999, 1.001, n)).astype(F)
+    ow = rng.uniform(-50, 50, (n, 3)).astype(F)
+    cases.append((cw, rw, ow, unit(rng.normal(size=(n, 3)))))
+    co = (rng.uniform(-1, 1, (n, 3)) + 3e4).astype(F)
+    cases.append((co, r, (co + rng.uniform(-3, 3, (n, 3))).astype(F), unit(rng.normal(size=(n, 3)))))
+    culled = 0
+    for c_, r_, o_, d_ in cases:
+        miss = pretest_miss(c_, r_, o_, d_)
+        det = fp64_det(c_, r_, o_, d_)
+        assert not np.any(miss & (det >= 0)), np.nonzero(miss & (det >= 0))[0][:5]
+        culled += int(miss.sum())
+    # It must also do its job: most rays of the first case miss their sphere.
+    assert culled > 0.5 * n

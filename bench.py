@@ -11,8 +11,9 @@ resident in HBM.  `e2e` is the same metric through ckr_trace_closest_host with p
 host buffers (ray upload and hit download inside the timed region).  Rank 0 prints one
 JSON line.  Under torchrun each rank traces its own copy of the batch (weak scaling, no
 data-path collective).  `--impl reference` times the reference's CPU traversal
-(BvhAccel::intersectT) on the host cores: its FP64 restatement in oracle/ (the reference
-binary itself cannot run on this host), each step a bounded sample of the batch.
+(BvhAccel::intersectT) on the host cores: its FP64 restatement in oracle/, on inputs made
+by the oracle's own generator (that process never loads libckr.so), the full batch per
+step unless the run would exceed a few minutes.
 """
 from __future__ import annotations
 
@@ -123,64 +124,114 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def build_oracle_only():
+    """Compiles oracle/liboracle.so (the FP64 C restatement) with make, without
+    importing the package, so that a process which only times the CPU port never
+    loads libckr.so."""
+    r = subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), f"-j{min(16, os.cpu_count() or 4)}", "all"],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise SystemExit(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+
+
+def make_workload_oracle():
+    """The same inputs as make_workload(), generated by the oracle's C restatement
+    (byte-identical to ckr_workload_*, checked by tests/test_workloads.py)."""
+    import oracle as O
+
+    tri = O.icosphere(8, 0.05, 6, 1)
+    lo, hi = tri.reshape(-1, 3).min(0), tri.reshape(-1, 3).max(0)
+    primary = O.rays_pinhole([0, 0, 3], [0, 0, 0], [0, 1, 0], 40.0, 2048, 2048)
+    incoh = O.rays_incoherent(lo, hi, 7, NRAYS_HALF, 0.05, 2.0)
+    closest = np.concatenate([primary, incoh])
+    closest[:, 7] = 1e30
+    return tri, closest
+
+
+def bench_config(n_rays: int, ntri: int, world: int) -> dict:
+    """The workload's config; identical in both arms."""
+    return {"workload": WORKLOAD, "rays_per_step": n_rays, "triangles": ntri,
+            "l2": "inputs larger than L2 (rays 256 MiB), no flush", "parallelism": f"replica x{world}"}
+
+
+REF_BUDGET_S = 180.0  # whole --impl reference run (warm-up + timed steps)
+
+
 def run_reference(args, rank, world):
-    """CPU arm: the reference's traversal on the host cores (FP64 restatement of
-    BvhAccel::intersectT over the reference's midpoint BVH)."""
+    """CPU arm: the reference's closest-hit traversal (BvhAccel::intersectT over its
+    midpoint BVH, src/bvhAccel.cpp:13-249) on all host cores, as the oracle's FP64
+    restatement (the reference's own objects are x86 builds from sources that are not
+    on the GPU host).  Inputs come from the oracle's generator: this process loads
+    only oracle/liboracle.so.  Each step traces the full 2^23-ray batch unless the
+    projected run exceeds REF_BUDGET_S, in which case later steps trace a stride
+    sample (reported in config and cpu_baseline)."""
     if rank != 0:
         return
     sys.path.insert(0, str(ROOT / "oracle"))
-    from chakumrender_gb300 import build
-
-    build.build_library()
-    build.build_oracle()
+    build_oracle_only()
     import oracle as O
 
-    tri, closest, _ = make_workload()
+    tri, closest = make_workload_oracle()
     cores = os.cpu_count() or 1
-    sample_n = 1 << 18  # rays per step: a stride sample over both halves of the batch
-    stride = len(closest) // sample_n
     t0 = time.perf_counter()
     ob = O.OracleBvh(tri)
     build_s = time.perf_counter() - t0
+    n = len(closest)
+    t0 = time.perf_counter()
+    ob.closest(closest, threads=cores)  # first warm-up step, full batch
+    t_full = time.perf_counter() - t0
+    total = args.warmup + args.steps
+    rays = closest
+    if t_full * total > REF_BUDGET_S:
+        stride = 1
+        while t_full / stride * (total - 1) + t_full > REF_BUDGET_S:
+            stride *= 2
+        rays = np.ascontiguousarray(closest[::stride])
     times = []
-    for k in range(args.warmup + args.steps):
-        rays = np.ascontiguousarray(closest[(k % stride)::stride][:sample_n])
+    for k in range(1, total):
         t0 = time.perf_counter()
         ob.closest(rays, threads=cores)
         dt = time.perf_counter() - t0
         if k >= args.warmup:
             times.append(dt)
-    mrays = sample_n * len(times) / sum(times) / 1e6
+    if args.warmup == 0:
+        times.insert(0, t_full)
+    m = len(rays)
+    full = m == n
+    sample = ("full 2^23-ray batch every step" if full else
+              f"{m} rays per step (stride-{n // m} sample of the 2^23-ray batch; the full batch took {t_full:.2f} s)")
+    mrays = m * len(times) / sum(times) / 1e6
     line = {"impl": "reference", "metric": METRIC, "value": round(mrays, 4), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample_rays_per_step": sample_n, "bvh_build_s": round(build_s, 3)},
+            "config": bench_config(n if full else m, len(tri), world),
+            "structure": {"bvh": f"the reference's midpoint BVH, one triangle per leaf ({ob.node_count()} nodes)",
+                          "bvh_build_s": round(build_s, 3)},
             "cpu_baseline": {"value": round(mrays, 4), "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{sample_n} rays per step (stride-{stride} sample of the 2^23-ray batch)"},
+                             "sample": sample + "; FP64 restatement of BvhAccel::intersectT, inputs from the "
+                                                "oracle's generator"},
             "e2e": {"value": round(mrays, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
 def cpu_baseline(tri, closest):
-    """The oracle port of the reference traversal on the host cores, bounded sample."""
+    """The oracle port of the reference traversal on the host cores over the full
+    2^23-ray batch (one pass, about 1.5 s on 16 cores), with per-ray node and
+    triangle counts of the reference's midpoint BVH."""
     sys.path.insert(0, str(ROOT / "oracle"))
-    from chakumrender_gb300 import build
-
-    build.build_oracle()
+    build_oracle_only()
     import oracle as O
 
     cores = os.cpu_count() or 1
     ob = O.OracleBvh(tri)
-    n = 1 << 20
-    stride = len(closest) // n
-    rays = np.ascontiguousarray(closest[::stride][:n])
+    n = len(closest)
     t0 = time.perf_counter()
-    _, _, nv, nt = ob.closest(rays, threads=cores, counts=True)
+    _, _, nv, nt = ob.closest(closest, threads=cores, counts=True)
     dt = time.perf_counter() - t0
     half = n // 2
     return ({"value": round(n / dt / 1e6, 4), "unit": UNIT, "cores": cores, "kind": "port",
-             "sample": f"{n} rays (stride-{stride} sample of the 2^23-ray batch), FP64 restatement of "
-                       f"BvhAccel::intersectT over the reference's midpoint BVH"},
+             "sample": f"the full {n}-ray batch, one pass, FP64 restatement of BvhAccel::intersectT over the "
+                       f"reference's midpoint BVH (with per-ray visit counters)"},
             {"primary": [float(nv[:half].mean()), float(nt[:half].mean())],
              "incoherent": [float(nv[half:].mean()), float(nt[half:].mean())]})
 
@@ -685,12 +736,11 @@ def main():
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "rays_per_step": n, "triangles": int(info.ntri),
-                   "bvh": (f"binned SAH to single triangles ({info.nnodes_binary} binary nodes), SAH-optimal "
-                           f"collapse to 8-wide nodes with 8-bit quantised boxes and leaves <= {min(args.leaf, 3)}: "
-                           f"{info.nnodes} wide nodes, depth {info.max_depth}"),
-                   "bvh_build_ms": round(info.build_ms, 1), "l2": "inputs larger than L2 (rays 256 MiB), no flush",
-                   "parallelism": f"replica x{world}"},
+        "config": bench_config(n, int(info.ntri), world),
+        "structure": {"bvh": (f"binned SAH to single triangles ({info.nnodes_binary} binary nodes), SAH-optimal "
+                              f"collapse to 8-wide nodes with 8-bit quantised boxes and leaves <= "
+                              f"{min(args.leaf, 3)}: {info.nnodes} wide nodes, depth {info.max_depth}"),
+                      "bvh_build_ms": round(info.build_ms, 1)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
                      "bytes_per_ray": round(bytes_per_ray, 1), "mean_wide_nodes": round(mean_nodes, 2),

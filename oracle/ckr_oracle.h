@@ -140,6 +140,21 @@ int orc_mlp_loss_grad(const double *params, const float *rec12, uint32_t n, cons
 void orc_mlp_adam(double *params, double *m, double *v, const double *grad, uint32_t n, uint32_t step, double lr,
                   double beta1, double beta2, double eps);
 
+/* ---------------------------------------------------------------------- */
+/* The synthetic traversal workload (orc_workload.c; no reference          */
+/* counterpart): byte-identical to the library's ckr_workload_* outputs.   */
+/* ---------------------------------------------------------------------- */
+/* Icosphere with subdiv levels, radially displaced by fractal value noise;
+ * tri9_out NULL: size query.  0 on success, negative on error. */
+int orc_workload_icosphere(uint32_t subdiv, float noise_amp, uint32_t octaves, uint64_t seed, float *tri9_out,
+                           uint32_t capacity, uint32_t *ntri_out);
+/* width x height pinhole rays (8 floats each), top row first. */
+int orc_workload_rays_pinhole(const float eye[3], const float target[3], const float up[3], float vfov_deg,
+                              uint32_t width, uint32_t height, float tmax, float *rays8);
+/* n rays with origins uniform in [lo, hi] and directions uniform on the sphere. */
+int orc_workload_rays_incoherent(const float lo[3], const float hi[3], uint64_t seed, uint32_t n, float tmax_lo,
+                                 float tmax_hi, float *rays8);
+
 /* One direction sample from uniforms (e1, e2); see orc_shading.c for `kind`. */
 void orc_sample_dir(int kind, const double *n3, const double *w3, double param, double e1, double e2, double *out3);
 

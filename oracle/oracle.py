@@ -51,6 +51,9 @@ def orc() -> C.CDLL:
         _sig(L, "orc_brdf_batch", [P, U32, P, P, P, P, C.c_int, P, P], None)
         _sig(L, "orc_ltc_shade_batch", [P, U32, P, P, P, P, P, U32, P, C.c_int], None)
         _sig(L, "orc_sample_dir", [C.c_int, P, P, C.c_double, C.c_double, C.c_double, P], None)
+        _sig(L, "orc_workload_icosphere", [U32, C.c_float, U32, C.c_uint64, P, U32, C.POINTER(U32)])
+        _sig(L, "orc_workload_rays_pinhole", [P, P, P, C.c_float, U32, U32, C.c_float, P])
+        _sig(L, "orc_workload_rays_incoherent", [P, P, C.c_uint64, U32, C.c_float, C.c_float, P])
         _sig(L, "orc_ltc_mc", [P, U32, P, P, P, P, P, U32, U32, C.c_uint64, P, P, C.c_int], None)
         _sig(L, "orc_mlp_forward", [P, P, U32, P, C.c_double, U32, P], None)
         _sig(L, "orc_mlp_loss_grad", [P, P, U32, P, C.c_double, U32, P, P], C.c_int)
@@ -82,6 +85,33 @@ def ref() -> C.CDLL:
 def _p(a: np.ndarray) -> int:
     assert a.flags["C_CONTIGUOUS"]
     return a.ctypes.data
+
+
+def icosphere(subdiv: int = 8, noise_amp: float = 0.05, octaves: int = 6, seed: int = 1) -> np.ndarray:
+    """The displaced icosphere of the traversal workload, made without the library."""
+    n = C.c_uint32(0)
+    if orc().orc_workload_icosphere(subdiv, noise_amp, octaves, seed, None, 0, C.byref(n)) != 0:
+        raise ValueError("icosphere size")
+    out = np.empty((n.value, 9), dtype=np.float32)
+    if orc().orc_workload_icosphere(subdiv, noise_amp, octaves, seed, _p(out), n.value, C.byref(n)) != 0:
+        raise RuntimeError("orc_workload_icosphere failed")
+    return out
+
+
+def rays_pinhole(eye, target, up, vfov_deg: float, width: int, height: int, tmax: float = 1e30) -> np.ndarray:
+    e, t, u = (np.ascontiguousarray(x, dtype=np.float32) for x in (eye, target, up))
+    out = np.empty((width * height, 8), dtype=np.float32)
+    if orc().orc_workload_rays_pinhole(_p(e), _p(t), _p(u), vfov_deg, width, height, tmax, _p(out)) != 0:
+        raise ValueError("orc_workload_rays_pinhole: invalid camera")
+    return out
+
+
+def rays_incoherent(lo, hi, seed: int, n: int, tmax_lo: float = 1e30, tmax_hi: float = 1e30) -> np.ndarray:
+    lo, hi = (np.ascontiguousarray(x, dtype=np.float32) for x in (lo, hi))
+    out = np.empty((n, 8), dtype=np.float32)
+    if orc().orc_workload_rays_incoherent(_p(lo), _p(hi), seed, n, tmax_lo, tmax_hi, _p(out)) != 0:
+        raise ValueError("orc_workload_rays_incoherent")
+    return out
 
 
 class OracleBvh:

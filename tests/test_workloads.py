@@ -55,3 +55,24 @@ def test_rng_stream():
     assert xs.min() >= 0 and xs.max() < 1
     assert abs(xs.mean() - 0.5) < 0.02
     assert np.all(xs * 16777216 == np.floor(xs * 16777216))  # 24-bit values
+
+
+def test_oracle_generator_is_byte_identical():
+    """The oracle's C restatement of the workload (used by the CPU timing of the
+    reference traversal, which must not load the library) gives the same bytes as
+    ckr_workload_*."""
+    import oracle as O
+
+    for sub, seed in ((0, 1), (3, 7), (5, 1)):
+        assert np.array_equal(ckr.icosphere(sub, 0.05, 6, seed).view(np.uint32),
+                              O.icosphere(sub, 0.05, 6, seed).view(np.uint32))
+    a = ckr.rays_pinhole([0, 0, 3], [0, 0, 0], [0, 1, 0], 40.0, 96, 64)
+    b = O.rays_pinhole([0, 0, 3], [0, 0, 0], [0, 1, 0], 40.0, 96, 64)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    lo, hi = np.array([-1.05, -1.04, -1.03], np.float32), np.array([1.02, 1.05, 1.01], np.float32)
+    a = ckr.rays_incoherent(lo, hi, 7, 50000, 0.05, 2.0)
+    b = O.rays_incoherent(lo, hi, 7, 50000, 0.05, 2.0)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    a = ckr.rays_incoherent(lo, hi, 7, 50000)
+    b = O.rays_incoherent(lo, hi, 7, 50000)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))

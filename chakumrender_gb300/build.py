@@ -20,7 +20,10 @@ BUILD = PKG / "_build"
 LIB = PKG / "libckr.so"
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
+HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fvisibility=hidden", "-fvisibility-inlines-hidden",
+              "-Wall"]
+# Exports: the ckr_* entry points the headers under include/ declare, nothing else.
+VERSION_SCRIPT = PKG / "csrc" / "exports.map"
 
 
 def _nvcc() -> str:
@@ -29,7 +32,7 @@ def _nvcc() -> str:
 
 
 def _headers_mtime() -> float:
-    hs = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
+    hs = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h")) + [VERSION_SCRIPT]
     return max((h.stat().st_mtime for h in hs), default=0.0)
 
 
@@ -37,7 +40,7 @@ def _compile_cmd(src: Path, obj: Path) -> list[str]:
     inc = ["-I", str(ROOT / "include"), "-I", str(CSRC)]
     if src.suffix == ".cu":
         return [_nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "--expt-relaxed-constexpr",
-                "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-warn-spills",
+                "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden,-fvisibility-inlines-hidden", "-Xptxas", "-warn-spills",
                 *inc, "-c", str(src), "-o", str(obj)]
     return ["g++", *HOST_FLAGS, *inc, "-I", str(CUDA_HOME / "include"), "-c", str(src), "-o", str(obj)]
 
@@ -70,7 +73,8 @@ def build_library(verbose: bool = False, jobs: int | None = None) -> Path:
     newest = max(Path(o).stat().st_mtime for o in objs)
     if todo or not LIB.exists() or LIB.stat().st_mtime < newest:
         tmp = LIB.with_suffix(".so.tmp")
-        cmd = [_nvcc(), *ARCH, "-shared", "-o", str(tmp), *objs, "-lpthread"]
+        cmd = [_nvcc(), *ARCH, "-shared", "-o", str(tmp), *objs, "-lpthread",
+               "-Xlinker", f"--version-script={VERSION_SCRIPT}"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
@@ -80,14 +84,26 @@ def build_library(verbose: bool = False, jobs: int | None = None) -> Path:
     return LIB
 
 
+def reference_checkout() -> Path | None:
+    """The reference checkout named by the CKR_REFERENCE environment variable, if it
+    holds the reference's sources (there is no default location)."""
+    ref = os.environ.get("CKR_REFERENCE")
+    if ref and (Path(ref) / "src" / "bvhAccel.cpp").exists():
+        return Path(ref)
+    return None
+
+
 def build_oracle(verbose: bool = False) -> None:
-    """Builds oracle/liboracle.so, and oracle/_ref/ where the reference sources exist."""
+    """Builds oracle/liboracle.so, and oracle/_ref/ when CKR_REFERENCE names the
+    reference's sources."""
     odir = ROOT / "oracle"
     targets = ["all"]
-    ref = Path(os.environ.get("CKR_REFERENCE", "/root/reference"))
-    if (ref / "src" / "bvhAccel.cpp").exists():
+    ref = reference_checkout()
+    extra = []
+    if ref is not None:
         targets.append("ref")
-    cmd = ["make", "-s", "-C", str(odir), f"-j{min(16, os.cpu_count() or 4)}", f"REF={ref}", *targets]
+        extra = [f"REF={ref}"]
+    cmd = ["make", "-s", "-C", str(odir), f"-j{min(16, os.cpu_count() or 4)}", *extra, *targets]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -26,6 +26,13 @@ struct BatchWs {
   DevBuf<unsigned long long> stats;
   DevBuf<float> hit_t;
   size_t wave = 0, shadow = 0;
+  // Frees the per-wave buffers (after a reserve that did not fit, so that a smaller
+  // wave is tried against all of device memory).
+  void release_waves() {
+    ray_o.release(), ray_d.release(), beta.release(), meta.release(), hit_id.release(), hit_t.release();
+    q0.release(), q1.release(), sh_o.release(), sh_d.release(), sh_c.release(), sh_px.release();
+    wave = shadow = 0;
+  }
   int reserve(size_t w, size_t per_path) {
     size_t sh = w * per_path;
     if (ray_o.reserve(w) || ray_d.reserve(w) || beta.reserve(w) || meta.reserve(w) || hit_id.reserve(w) ||
@@ -210,7 +217,9 @@ int enqueue_any(ckr_batch *b, JobSet &set, bool pack, const ckr_batch_tuning &t,
 }
 
 // Times block x wave candidates on the batch with spp capped at 1 (outputs to a
-// scratch image) and keeps the fastest.
+// scratch image) and keeps the fastest.  A wave whose workspace does not fit in
+// device memory ends that block size's sweep (larger waves need more); the
+// tuner fails only when no candidate fits at all.
 int autotune(ckr_batch *b, ckr_batch_tuning *best) {
   std::vector<float *> scratch(b->job_in.size(), nullptr);
   uint32_t maxpix = 0;
@@ -232,7 +241,13 @@ int autotune(ckr_batch *b, ckr_batch_tuning *best) {
     for (uint32_t w = 1u << 17; w <= (1u << 21); w <<= 1) {
       if (w > 2 * small.paths && w > (1u << 17)) break;
       ckr_batch_tuning t{blk, w, 0.f, 0};
-      if ((st = b->ws.reserve(w, b->per_path)) != CKR_OK) break;
+      if ((st = b->ws.reserve(w, b->per_path)) != CKR_OK) {
+        if (st != CKR_ERR_OUT_OF_MEMORY) break;
+        (void)cudaGetLastError();  // the failed allocation's error is not sticky
+        b->ws.release_waves();
+        st = CKR_OK;
+        break;  // next block size
+      }
       if ((st = enqueue_any(b, small, true, t, s, nullptr)) != CKR_OK) break;  // warm-up
       CKR_CUDA_TRY(cudaEventRecord(e0, s));
       if ((st = enqueue_any(b, small, true, t, s, nullptr)) != CKR_OK) break;
@@ -251,6 +266,7 @@ int autotune(ckr_batch *b, ckr_batch_tuning *best) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (st == CKR_OK && best->candidates == 0) st = CKR_ERR_OUT_OF_MEMORY;
   return st;
 }
 

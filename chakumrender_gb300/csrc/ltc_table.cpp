@@ -15,6 +15,7 @@
 #include <string>
 
 #include "ckr_internal.h"
+#include "ckr_test.h"
 
 namespace ckr {
 

@@ -6,6 +6,7 @@
 #include <cstring>
 #include <vector>
 
+#include "ckr_test.h"
 #include "proposal.h"
 #include "scene.h"
 

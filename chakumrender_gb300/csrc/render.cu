@@ -370,11 +370,11 @@ extern "C" int ckr_render_host(ckr_scene *s, const ckr_camera *cam, const ckr_re
 
 // ---- rendering from a static arena (no device allocation) -------------------
 //
-// For callers that may not allocate device memory while they render: code that
-// runs during CUDA stream capture (cudaMalloc / cudaFree are not capturable and
-// may synchronise the device), frame loops that cannot afford the implicit
-// synchronisation of an allocation, and hosts whose device memory is owned by
-// their own allocator.  ckr_render_noalloc runs the same kernels as ckr_render,
+// For callers that cannot call cudaMalloc while they render: renderers embedded
+// in a host application whose device memory comes only from the host's own pool,
+// frame loops that cannot afford the device-wide synchronisation an allocation
+// or a free may cause, and processes so close to the memory limit that an
+// allocation in the middle of a frame could fail.  ckr_render_noalloc runs the same kernels as ckr_render,
 // but its scratch memory (path state, path and shadow-ray queues, FP64 sums,
 // a copy of the LTC table) lives in file-scope device arrays that every GPU
 // loading the library holds until the process exits.
@@ -421,13 +421,14 @@ int noalloc_setup(int dev) {
 
 extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb,
                                   void *stream_) {
-  if (!s || !cam || !cfg || !rgb || cam->width == 0 || cam->height == 0 || cfg->spp == 0 || cfg->shader > 4)
+  if (!s || !cam || !cfg || !rgb || cam->width == 0 || cam->height == 0 || cfg->spp == 0 || cfg->shader > 5)
     return CKR_ERR_INVALID_ARGUMENT;
   if (!s->has_shading) return CKR_ERR_INVALID_ARGUMENT;
   if (cfg->max_depth > 60 || cfg->spp > 65536 || cfg->n_light_samples > 256 || cfg->n_brdf_samples > 256)
     return CKR_ERR_TOO_LARGE;
   if ((uint64_t)cam->width * cam->height > kNoAllocMaxPixels) return CKR_ERR_TOO_LARGE;
   cudaStream_t stream = (cudaStream_t)stream_;
+  std::lock_guard<std::mutex> scene_lock(s->host_mu);
   int dev = 0;
   CKR_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return CKR_ERR_INVALID_ARGUMENT;
@@ -436,11 +437,12 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
   Params prm{};
   prm.shader = cfg->shader;
   prm.spp = cfg->spp;
-  const bool path = cfg->shader == CKR_SHADER_PATH || cfg->shader == CKR_SHADER_PATH_NEE;
+  const bool path = cfg->shader == CKR_SHADER_PATH || cfg->shader == CKR_SHADER_PATH_NEE ||
+                    cfg->shader == CKR_SHADER_EXPLICIT;
   if (cfg->shader == CKR_SHADER_PATH_NEE && s->n_emit == 0) return CKR_ERR_INVALID_ARGUMENT;
   prm.max_depth = path ? std::max(1u, cfg->max_depth) : 1u;
   prm.n_light = cfg->n_light_samples;
-  prm.n_brdf = path ? 1u : cfg->n_brdf_samples;
+  prm.n_brdf = path && cfg->shader != CKR_SHADER_EXPLICIT ? 1u : cfg->n_brdf_samples;
   prm.rr_prob = path ? cfg->rr_prob : 0.f;
   prm.seed = cfg->seed;
   prm.npix = cam->width * cam->height;
@@ -452,6 +454,7 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
                                 (cfg->shader == CKR_SHADER_DIRECT_MIS ? prm.n_brdf : 0) +
                                 (cfg->shader == CKR_SHADER_DIRECT_MIS || cfg->shader == CKR_SHADER_PATH ? s->env_n : 0);
   if (cfg->shader == CKR_SHADER_DIRECT_CV) per_path = (uint64_t)mesh_lights_of(s) * prm.n_light;
+  if (cfg->shader == CKR_SHADER_EXPLICIT) per_path = 0;  // the MISCV direct term traces no shadow rays
   if (per_path > kNoAllocShadow) return CKR_ERR_TOO_LARGE;
   prm.shadow_per_path = (uint32_t)std::max<uint64_t>(1, per_path);
   uint64_t total = (uint64_t)prm.npix * prm.spp;
@@ -506,12 +509,16 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
   }
   const int g_ext = grid_for((const void *)extend_fn, smem, kRTPB);
   const int g_sh = grid_for((const void *)shadow_fn, smem, kRTPB);
-  const void *shade_fn = cfg->shader == CKR_SHADER_PATH_NEE ? (const void *)k_shade_nee<kRTPB>
+  if (cfg->shader == CKR_SHADER_EXPLICIT && smem > 48 * 1024)
+    CKR_CUDA_TRY(cudaFuncSetAttribute(k_shade<CKR_SHADER_EXPLICIT, kRTPB>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const void *shade_fn = cfg->shader == CKR_SHADER_EXPLICIT ? (const void *)k_shade<CKR_SHADER_EXPLICIT, kRTPB>
+                         : cfg->shader == CKR_SHADER_PATH_NEE ? (const void *)k_shade_nee<kRTPB>
                          : cfg->shader == CKR_SHADER_PATH      ? (const void *)k_shade_path<kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_CV  ? (const void *)k_shade<CKR_SHADER_DIRECT_CV, kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_MIS ? (const void *)k_shade<CKR_SHADER_DIRECT_MIS, kRTPB>
                                                                 : (const void *)k_shade_miscv<kRTPB>;
-  const int g_shade = grid_for(shade_fn, 0, kRTPB);
+  const int g_shade = grid_for(shade_fn, cfg->shader == CKR_SHADER_EXPLICIT ? smem : 0, kRTPB);
   for (uint64_t base = 0; base < total; base += wave) {
     uint32_t n = (uint32_t)std::min<uint64_t>(wave, total - base);
     k_camera<kRTPB><<<std::min<int>(g_ext, ceil_div(n, kRTPB)), kRTPB, 0, stream>>>(c, P, prm, base, n);
@@ -522,7 +529,10 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
       extend_fn<<<g_ext, kRTPB, smem, stream>>>(sv, P, cur, depth);
       CKR_CUDA_TRY(cudaMemsetAsync(P.counts + (cur ^ 1), 0, sizeof(uint32_t), stream));
       CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), stream));
-      if (cfg->shader == CKR_SHADER_PATH_NEE)
+      if (cfg->shader == CKR_SHADER_EXPLICIT)
+        k_shade<CKR_SHADER_EXPLICIT, kRTPB><<<g_shade, kRTPB, smem, stream>>>(shv, P, prm, cur, (int)d, ltc, sv,
+                                                                              depth);
+      else if (cfg->shader == CKR_SHADER_PATH_NEE)
         k_shade_nee<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, Learn{});
       else if (cfg->shader == CKR_SHADER_PATH)
         k_shade_path<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);

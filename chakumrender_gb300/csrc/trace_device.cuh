@@ -129,14 +129,17 @@ __device__ __forceinline__ double hit_sphere(const RayPre &r, float4 s) {
     // FP32 pre-test (FP64 is slow on this part): a ray whose line passes the sphere
     // by more than 1e-5 of the squared magnitudes involved -- orders of magnitude
     // above the FP32 rounding of these few operations -- has a negative FP64
-    // discriminant too, so the miss is decided without FP64.  NaN and overflow fall
+    // discriminant too, so the miss is decided without FP64.  The rounding of b =
+    // (c - o).d grows with |d|, so the bound scales the (c - o) terms by
+    // max(1, |d|^2): directions need not have unit length.  NaN and overflow fall
     // through to the FP64 test.
     const float ox = s.x - r.ox, oy = s.y - r.oy, oz = s.z - r.oz;
     const float b = ox * r.dx + oy * r.dy + oz * r.dz;
     const float oo = ox * ox + oy * oy + oz * oz;
+    const float dd = fmaxf(1.f, r.dx * r.dx + r.dy * r.dy + r.dz * r.dz);
     const float m = fmaxf(fmaxf(fmaxf(fabsf(s.x), fabsf(s.y)), fabsf(s.z)),
                           fmaxf(fmaxf(fabsf(r.ox), fabsf(r.oy)), fabsf(r.oz)));
-    if (b * b - oo + s.w * s.w < -1e-5f * (m * m + oo + b * b + s.w * s.w)) return 1e300;
+    if (b * b - oo + s.w * s.w < -1e-5f * ((m * m + oo) * dd + b * b + s.w * s.w)) return 1e300;
   }
   double opx = (double)s.x - r.ox, opy = (double)s.y - r.oy, opz = (double)s.z - r.oz;
   double dx = r.dx, dy = r.dy, dz = r.dz;

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/ckr.h"
+#include "../../include/ckr_test.h"
 #include "bvh_build.h"
 
 namespace ckr {

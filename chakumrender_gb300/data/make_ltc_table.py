@@ -54,4 +54,6 @@ def main(src: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/headers/ltc.inc")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_ltc_table.py <reference checkout>/headers/ltc.inc")
+    main(sys.argv[1])

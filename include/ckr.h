@@ -24,6 +24,11 @@
 #ifdef __cplusplus
 extern "C" {
 #endif
+/* The library is built with hidden visibility; what this header declares is
+ * its exported interface. */
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
 
 /* ---- status codes ------------------------------------------------------ */
 #define CKR_OK 0
@@ -259,12 +264,18 @@ int ckr_render(ckr_scene *scene, const ckr_camera *cam, const ckr_render_cfg *cf
                void *stream);
 
 /* Rendering that allocates no device memory.  No counterpart in the reference:
- * it exists for callers that must not allocate while they render, such as code
- * running inside CUDA stream capture (cudaMalloc / cudaFree cannot be captured
- * and may synchronise the device), frame loops that cannot take an allocation's
- * implicit synchronisation, and hosts whose device memory belongs to their own
- * allocator.  Same result as ckr_render with accum = NULL (up to the order of
- * the FP64 sums); the scene must already exist.  All scratch memory (path
+ * it exists for callers that cannot call cudaMalloc while they render: a
+ * renderer embedded in a host application (an engine or a content tool) whose
+ * device memory is handed out only by the host's own pool, real-time frame
+ * loops that cannot take the device-wide synchronisation a cudaMalloc or
+ * cudaFree may cause, and processes running so close to the memory limit that
+ * an allocation in the middle of a frame could fail.  Same result as ckr_render with accum = NULL (up to the order of
+ * the FP64 sums), for every shader; the scene must already exist.  Path
+ * tracers run in fixed waves here (ckr_render may regenerate paths instead),
+ * which changes only the order of the FP64 sums.  Like ckr_render it does not
+ * wait for the GPU: traversal errors (a stack overflow, an iteration limit)
+ * land in the scene's device status word, which the caller reads with
+ * ckr_scene_check after the stream has run the call.  All scratch memory (path
  * state, queues, shadow rays, FP64 sums, an LTC table copy) lives in one
  * static device arena of 16 MiB plus 192 KiB, which every GPU that loads the
  * library holds until the process exits.  Limits: width * height <= 262144
@@ -510,6 +521,9 @@ int ckr_workload_manylight(const ckr_manylight_spec *spec, float *tri9, uint32_t
 /* The library's counter-based stream (see csrc/ckr_rng.h), for checkers. */
 float ckr_rng_uniform(uint64_t seed, uint64_t index, uint32_t counter);
 
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
 #ifdef __cplusplus
 }
 #endif

@@ -1,9 +1,10 @@
 """Generates the golden fixtures in tests/golden/ by running the REFERENCE renderer.
 
-Needs oracle/_ref/libckr_ref.so (built by `make -C oracle ref` from the reference's own
-sources) and libckr.so (for the deterministic input generators).  Run from the repo root:
+Needs oracle/_ref/libckr_ref.so (built by `make -C oracle ref REF=<checkout>` from the
+reference's own sources) and libckr.so (for the deterministic input generators).  Run
+from the repo root with CKR_REFERENCE naming the reference checkout:
 
-    python tests/golden/make_golden.py
+    CKR_REFERENCE=<checkout> python tests/golden/make_golden.py
 
 Fixtures:
   trace_small.npz        1280-triangle displaced icosphere; pinhole + incoherent rays;
@@ -17,6 +18,7 @@ Fixtures:
 from __future__ import annotations
 
 import hashlib
+import os
 import sys
 from pathlib import Path
 
@@ -30,6 +32,7 @@ from chakumrender_gb300 import ckr  # noqa: E402
 import oracle as O  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
+REFERENCE = Path(os.environ.get("CKR_REFERENCE", "")) if os.environ.get("CKR_REFERENCE") else None
 
 
 def ray(o, d, tmax=1e30, tmin=0.0):
@@ -161,7 +164,7 @@ def reference_images():
 
     exe = ROOT / "oracle" / "_ref" / "a.out"
     scenes = {"box": ROOT / "chakumrender_gb300" / "scenes" / "box.xml",
-              "scene0": Path("/root/reference/scene0.xml")}
+              "scene0": REFERENCE / "scene0.xml"}
     out = {}
     for name, xml in scenes.items():
         with tempfile.TemporaryDirectory() as d:
@@ -174,7 +177,9 @@ def reference_images():
 
 def main():
     if not O.ref_available():
-        sys.exit("oracle/_ref/libckr_ref.so is missing: run `make -C oracle ref` first")
+        sys.exit("oracle/_ref/libckr_ref.so is missing: run `make -C oracle ref REF=<checkout>` first")
+    if REFERENCE is None or not (REFERENCE / "scene0.xml").exists():
+        sys.exit("set CKR_REFERENCE to the reference checkout (its scene0.xml and scene1.xml are read)")
     np.savez_compressed(OUT / "ref_images.npz", **reference_images())
     print("reference images: written")
     # The reference's own scenes as parsed by the library's loader (which the CPU
@@ -186,7 +191,7 @@ def main():
 
     arrays = {}
     for name in ("scene0", "scene1"):
-        arrays.update(to_arrays(S.load_xml(f"/root/reference/{name}.xml"), name))
+        arrays.update(to_arrays(S.load_xml(str(REFERENCE / f"{name}.xml")), name))
     np.savez_compressed(OUT / "ref_scenes.npz", **arrays)
     print("reference scenes: written")
     np.savez_compressed(OUT / "shading.npz", **shading())

@@ -8,6 +8,8 @@ from __future__ import annotations
 import ctypes as C
 from pathlib import Path
 
+import os
+
 import numpy as np
 import pytest
 
@@ -16,7 +18,7 @@ from chakumrender_gb300 import scene as S
 from scene_io import block_agreement, from_arrays, same_scene, srgb8
 
 GOLD = Path(__file__).resolve().parent / "golden"
-REF = Path("/root/reference")
+REF = Path(os.environ.get("CKR_REFERENCE", "")) if os.environ.get("CKR_REFERENCE") else Path("/nonexistent")
 BOX = S.SCENES / "box.xml"
 
 

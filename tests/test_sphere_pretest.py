@@ -16,8 +16,10 @@ def pretest_miss(c, r, o, d):
     ox, oy, oz = (c[:, 0] - o[:, 0]), (c[:, 1] - o[:, 1]), (c[:, 2] - o[:, 2])
     b = ox * d[:, 0] + oy * d[:, 1] + oz * d[:, 2]
     oo = ox * ox + oy * oy + oz * oz
+    dd = np.maximum(F(1), d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
     m = np.maximum(np.abs(c).max(1), np.abs(o).max(1))
-    return b * b - oo + r * r < F(-1e-5) * (m * m + oo + b * b + r * r)
+    with np.errstate(over="ignore", invalid="ignore"):
+        return b * b - oo + r * r < F(-1e-5) * ((m * m + oo) * dd + b * b + r * r)
 
 
 def fp64_det(c, r, o, d):
@@ -53,6 +55,22 @@ def test_pretest_never_rejects_a_hit():
     cases.append((cw, rw, ow, unit(rng.normal(size=(n, 3)))))
     co = (rng.uniform(-1, 1, (n, 3)) + 3e4).astype(F)
     cases.append((co, r, (co + rng.uniform(-3, 3, (n, 3))).astype(F), unit(rng.normal(size=(n, 3)))))
+    # Directions of any length (the ABI does not require unit directions): |d| from
+    # 1e-3 to 1e3 on the random and grazing cases, and rays whose length |d| = s puts
+    # the reference's discriminant s^2 (op.u)^2 - |op|^2 + r^2 within 1e-7..1e-3 of 0.
+    for c_, r_, o_, d_ in list(cases[:2]):
+        s = (10 ** rng.uniform(-3, 3, n)).astype(F)[:, None]
+        cases.append((c_, r_, o_, (d_ * s).astype(F)))
+    op = (c - o).astype(np.float64)
+    oo_ = (op * op).sum(1)
+    s = 10 ** rng.uniform(0, 3, n)
+    cos = np.sqrt(np.maximum(oo_ - r.astype(np.float64) ** 2, 0)) / (s * np.sqrt(oo_))
+    ok = (oo_ > r.astype(np.float64) ** 2) & (cos < 1)
+    perp = np.cross(op, rng.normal(size=(n, 3)))
+    perp /= np.linalg.norm(perp, axis=1, keepdims=True)
+    u = op / np.sqrt(oo_)[:, None] * cos[:, None] + perp * np.sqrt(np.maximum(1 - cos * cos, 0))[:, None]
+    ds = u * (s * (1 + rng.choice([-1, 1], n) * 10 ** rng.uniform(-7, -3, n)))[:, None]
+    cases.append((c[ok], r[ok], o[ok], ds[ok].astype(F)))
     culled = 0
     for c_, r_, o_, d_ in cases:
         miss = pretest_miss(c_, r_, o_, d_)

@@ -1,7 +1,8 @@
-"""ckr_render_noalloc: rendering without device allocation, for callers that cannot
-allocate while they render (stream capture, frame loops, foreign allocators).  Its
-output must equal ckr_render's on the same scene, camera and streams, on two calls in a
-row (the second call reuses the static arena the first one left behind).
+"""ckr_render_noalloc: rendering without device allocation, for callers that cannot call
+cudaMalloc while they render (renderers embedded in a host that owns all device memory,
+frame loops that cannot take an allocation's synchronisation).  Its output must equal
+ckr_render's on the same scene, camera and streams, on two calls in a row (the second
+call reuses the static arena the first one left behind).
 
 This file sorts last so that a run stopping at the first failure has run everything
 else first."""
@@ -30,7 +31,8 @@ def noalloc(scene, cam, cfg, torch):
 
 @pytest.mark.parametrize("shader,spp,nl,nb,depth", [(S.SHADER_PATH, 16, 1, 1, 4),
                                                     (S.SHADER_DIRECT_MISCV, 2, 10, 60, 1),
-                                                    (S.SHADER_DIRECT_MIS, 2, 10, 60, 1)])
+                                                    (S.SHADER_DIRECT_MIS, 2, 10, 60, 1),
+                                                    (S.SHADER_EXPLICIT, 2, 10, 60, 4)])
 def test_noalloc_matches_render(torch_cuda, shader, spp, nl, nb, depth):
     sd = S.load_xml(S.SCENES / "box.xml")
     cam = sd.camera
@@ -40,6 +42,7 @@ def test_noalloc_matches_render(torch_cuda, shader, spp, nl, nb, depth):
     for _ in range(2):
         st, img = noalloc(scene, cam, cfg, torch_cuda)
         assert st == 0
+        assert scene.check_device(torch_cuda.cuda.current_stream().cuda_stream) == 0
         # The same tolerance as the renderer's determinism test: FP64 sums in another
         # order may change the last FP32 bit.
         assert np.allclose(img, ref, rtol=1e-6, atol=1e-7)

@@ -86,7 +86,7 @@ void free_ws(void *p) { delete static_cast<Workspace *>(p); }
 namespace {
 
 int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb,
-                double *accum, void *stream_) {
+                double *accum, void *stream_, const ckr_ray *rays = nullptr) {
   if (!s || !cam || !cfg || !rgb || cam->width == 0 || cam->height == 0 || cfg->spp == 0 || cfg->shader > 5)
     return CKR_ERR_INVALID_ARGUMENT;
   if (!s->has_shading) return CKR_ERR_INVALID_ARGUMENT;
@@ -113,6 +113,7 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   prm.rr_prob = path ? cfg->rr_prob : 0.f;
   prm.seed = cfg->seed;
   prm.npix = cam->width * cam->height;
+  prm.rays = reinterpret_cast<const float4 *>(rays);
   uint32_t area_lights = 0, point_lights = 0;
   for (const DevLight &L : s->host_lights) (L.type == CKR_LIGHT_POINT ? point_lights : area_lights)++;
   uint32_t per_path = cfg->shader == CKR_SHADER_PATH_NEE
@@ -331,6 +332,43 @@ extern "C" int ckr_render_learned(ckr_scene *s, ckr_proposal *prop, const ckr_ca
                                   float *rgb, double *accum, void *stream) {
   if (!prop) return CKR_ERR_INVALID_ARGUMENT;
   return render_impl(s, prop, cam, cfg, rgb, accum, stream);
+}
+
+extern "C" int ckr_shade_rays(ckr_scene *s, const ckr_ray *rays, uint32_t n, const ckr_render_cfg *cfg, float *rgb,
+                              void *stream) {
+  if (!s || !rays || !cfg || !rgb || n == 0 || (reinterpret_cast<uintptr_t>(rays) & 15u))
+    return CKR_ERR_INVALID_ARGUMENT;
+  ckr_camera cam{};
+  cam.width = n;  // one output row per ray: key (seed, i), pixel i of an n x 1 image
+  cam.height = 1;
+  return render_impl(s, nullptr, &cam, cfg, rgb, nullptr, stream, rays);
+}
+
+extern "C" int ckr_shade_rays_host(ckr_scene *s, const ckr_ray *rays, uint32_t n, const ckr_render_cfg *cfg,
+                                   float *rgb, void *stream) {
+  if (!s || !rays || !cfg || !rgb || n == 0) return CKR_ERR_INVALID_ARGUMENT;
+  cudaStream_t st_ = (cudaStream_t)stream;
+  ckr_ray *d_rays = nullptr;
+  float *d_rgb = nullptr;
+  CKR_CUDA_TRY(cudaMalloc((void **)&d_rays, n * sizeof(ckr_ray)));
+  int st = CKR_OK;
+  if (cudaMalloc((void **)&d_rgb, 3 * sizeof(float) * (size_t)n) != cudaSuccess) st = CKR_ERR_OUT_OF_MEMORY;
+  if (st == CKR_OK &&
+      cudaMemcpyAsync(d_rays, rays, n * sizeof(ckr_ray), cudaMemcpyHostToDevice, st_) != cudaSuccess)
+    st = CKR_ERR_CUDA;
+  if (st == CKR_OK) st = ckr_shade_rays(s, d_rays, n, cfg, d_rgb, stream);
+  if (st == CKR_OK) {
+    cudaError_t e = cudaMemcpyAsync(rgb, d_rgb, 3 * sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) st = CKR_ERR_CUDA;
+  }
+  cudaFree(d_rays);
+  cudaFree(d_rgb);
+  if (st == CKR_OK) {
+    int h = ckr_scene_check(s, stream);
+    if (h != 0) st = h;
+  }
+  return st;
 }
 
 extern "C" int ckr_render_stats(ckr_scene *s, uint64_t *closest_rays, uint64_t *shadow_rays, int reset) {

@@ -97,6 +97,10 @@ struct Params {
   // (0: off); cam is the camera of those paths.
   uint32_t regen_total;
   Cam cam;
+  // Caller rays (ckr_shade_rays): path g traces ray g % npix (two float4 per ray)
+  // as sample g / npix, keyed and accumulated as output row g % npix; nullptr:
+  // camera rays.
+  const float4 *rays;
 };
 
 // Per-path values that a batch takes from the path's job.
@@ -159,6 +163,16 @@ __device__ __forceinline__ void add_px(double *accum, uint32_t px, F3 c) {
 // slot `slot`.
 __device__ __forceinline__ void camera_path(const Cam &cam0, const Params &prm, const Paths &P, uint64_t g,
                                             uint32_t slot) {
+  if (prm.rays) {
+    const uint32_t sample = (uint32_t)(g / prm.npix), row = (uint32_t)(g % prm.npix);
+    const float4 o = prm.rays[2 * (size_t)row], d4 = prm.rays[2 * (size_t)row + 1];
+    const F3 d = normalize(f3(d4.x, d4.y, d4.z));  // shade() takes normalised directions
+    P.ray_o[slot] = make_float4(o.x, o.y, o.z, fmaxf(o.w, 0.f));  // a negative tmin marks explicit rays
+    P.ray_d[slot] = make_float4(d.x, d.y, d.z, d4.w);
+    P.beta[slot] = make_float4(1.f, 1.f, 1.f, 1.f);
+    P.meta[slot] = make_uint4(row, sample, 0u, 0u);
+    return;
+  }
   Cam cam = cam0;
   uint32_t npix = prm.npix, job = 0, px_base = 0;
   if (prm.jobs) {

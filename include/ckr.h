@@ -263,6 +263,20 @@ typedef struct ckr_render_cfg {
 int ckr_render(ckr_scene *scene, const ckr_camera *cam, const ckr_render_cfg *cfg, float *rgb, double *accum,
                void *stream);
 
+/* Shades caller rays: radiance along each ray by the configured shader, the
+ * mean over cfg->spp samples, 3 floats per ray into rgb (device).  This is
+ * shade() (headers/shader.h:4, src/shader.cpp:363-378) over a batch: ray i
+ * draws from the stream (cfg->seed, i) exactly as pixel i of ckr_render does,
+ * so rays equal to a camera's give that camera's image.  Directions are
+ * normalised on the device; rays (device) must be 16-byte aligned; tmin < 0
+ * counts as 0. */
+int ckr_shade_rays(ckr_scene *scene, const ckr_ray *rays, uint32_t n, const ckr_render_cfg *cfg, float *rgb,
+                   void *stream);
+/* The same with host buffers: copies in, shades, copies out, synchronises and
+ * returns the scene's device status (ckr_scene_check). */
+int ckr_shade_rays_host(ckr_scene *scene, const ckr_ray *rays, uint32_t n, const ckr_render_cfg *cfg, float *rgb,
+                        void *stream);
+
 /* Rendering that allocates no device memory.  No counterpart in the reference:
  * it exists for callers that cannot call cudaMalloc while they render: a
  * renderer embedded in a host application (an engine or a content tool) whose

@@ -51,6 +51,7 @@ struct BatchWs {
     P.counts = counts.ptr;
     P.stats = stats.ptr;
     P.accum = accum;
+    P.sh_cap = (uint32_t)std::min<size_t>(shadow, 0xFFFFFFFFu);
     return P;
   }
 };
@@ -171,6 +172,7 @@ int enqueue(ckr_batch *b, JobSet &set, bool pack, size_t wave, cudaStream_t stre
   ShadeView shv = shade_view_of(s);
   shv.mats = b->mats.ptr;
   Paths P = b->ws.paths(b->accum.ptr);
+  P.status = b->scene->status.ptr;
   uint32_t n_launch = 0;
   CKR_CUDA_TRY(cudaMemsetAsync(b->accum.ptr, 0, sizeof(double) * 3 * (size_t)set.pixels, stream));
   // Path ranges: the whole batch, or one range per job.

@@ -73,6 +73,9 @@ __device__ __forceinline__ uint32_t rows(uint32_t n_max, const uint32_t *n_dev, 
 struct Params {
   float cx, cy, cz, scale;
   uint32_t nclusters;
+  // Test hook: when non-zero, the first layer's MMAs are not issued and every
+  // mbarrier wait gives up after this many polls (a phase nothing completes).
+  uint32_t stall_tries;
 };
 
 // Row features into the first-layer operand (K = 96).
@@ -188,14 +191,15 @@ __device__ __forceinline__ void sync_for_mma(uint32_t g) {
 
 // Waits for the group's committed MMAs; false (uniformly within the group) when
 // the wait gave up.
-__device__ __forceinline__ bool wait_mma(uint32_t g, uint32_t mbar, uint32_t &phase, int *abort, int *err) {
-  if (!tc::mbar_wait(mbar, phase, kWaitTries)) {
+__device__ __forceinline__ bool wait_mma(uint32_t g, uint32_t mbar, uint32_t &phase, int *abort, int *err,
+                                         uint32_t tries = kWaitTries) {
+  if (!tc::mbar_wait(mbar, phase, tries)) {
     *abort = 1;
     atomicExch(err, CKR_ERR_ITERATION_LIMIT);
   }
   group_sync(g);
   if (*abort) {
-    tc::mbar_wait(mbar, phase, kWaitTries);  // let the MMAs in flight land before TMEM is freed
+    tc::mbar_wait(mbar, phase, tries);  // let the MMAs in flight land before TMEM is freed
     return false;
   }
   phase ^= 1u;
@@ -325,13 +329,13 @@ __global__ void __launch_bounds__(kInferTPB, 2) k_mlp_infer(const float4 *__rest
     bool ok = true;
     for (int l = 0; l < 4 && ok; ++l) {
       sync_for_mma(g);
-      if (t == 0) {
+      if (t == 0 && !(p.stall_tries && l == 0)) {
         tc::fence_after_sync();
         if (l == 0) issue(tmem, a_addr, w_addr + kImgW1, kIn, 0);
         else issue(tmem, a_addr, w_addr + kImgW2 + 10240u * (l - 1), kHidK, 0);
         tc::mma_commit(mbar);
       }
-      ok = wait_mma(g, mbar, phase, &S.abort[g], err);
+      ok = wait_mma(g, mbar, phase, &S.abort[g], err, p.stall_tries ? p.stall_tries : kWaitTries);
       if (ok && l < 3) epilogue_relu(lane_addr, A, t);
       if (PATHS && l == 1) gather_hit(pr, nxt);
     }
@@ -658,6 +662,7 @@ Params params_of(const Net &net) {
   p.cz = net.centre[2];
   p.scale = net.scale;
   p.nclusters = net.nclusters;
+  p.stall_tries = net.stall_tries;
   return p;
 }
 

@@ -51,6 +51,7 @@ struct Net {
   uint32_t nclusters = 0;
   uint32_t step = 0;
   float lr = 1e-3f, beta1 = 0.9f, beta2 = 0.999f, eps = 1e-8f;
+  uint32_t stall_tries = 0;  // test hook of the bounded waits (0: off); see Params in mlp.cu
 };
 
 int create(Net &net, uint64_t seed);

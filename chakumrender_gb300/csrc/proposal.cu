@@ -106,6 +106,18 @@ extern "C" int ckr_proposal_infer(ckr_proposal *p, const float *rec12, uint32_t 
                     nullptr, p->defensive, (cudaStream_t)stream);
 }
 
+extern "C" int ckr_internal_proposal_infer_stalled(ckr_proposal *p, const float *rec12, uint32_t n, uint16_t *probs,
+                                                   uint32_t wait_tries, void *stream) {
+  if (!p || !n || !rec12 || !probs || wait_tries == 0 || ((uintptr_t)rec12 & 15u) || ((uintptr_t)probs & 15u))
+    return CKR_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(p->mu);
+  p->net.stall_tries = wait_tries;
+  int st = mlp::infer(p->net, reinterpret_cast<const float4 *>(rec12), n, nullptr, reinterpret_cast<__half *>(probs),
+                      nullptr, p->defensive, (cudaStream_t)stream);
+  p->net.stall_tries = 0;
+  return st;
+}
+
 extern "C" int ckr_proposal_train_step(ckr_proposal *p, const float *rec12, uint32_t n, void *stream) {
   if (!p || (n && !rec12) || ((uintptr_t)rec12 & 15u)) return CKR_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lock(p->mu);

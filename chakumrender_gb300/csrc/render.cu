@@ -24,6 +24,7 @@
 #include <algorithm>
 
 #include "ckr_internal.h"
+#include "ckr_test.h"
 #include "ltc_table.h"
 #include "mlp.h"
 #include "proposal.h"
@@ -162,6 +163,12 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   P.counts = W.counts.ptr;
   P.stats = W.stats.ptr;
   P.accum = acc;
+  P.sh_cap = (uint32_t)std::min<size_t>(shadow, 0xFFFFFFFFu);
+  P.status = s->status.ptr;
+  if (s->test_shadow_cap) {
+    P.sh_cap = std::min(P.sh_cap, s->test_shadow_cap);
+    s->test_shadow_cap = 0;
+  }
   bool train = prop && prop->train && (!prop->max_steps || prop->net.step < prop->max_steps);
   if (prop) {
     CKR_CUDA_TRY(prop->sel[0].reserve(64 * wave));
@@ -371,6 +378,13 @@ extern "C" int ckr_shade_rays_host(ckr_scene *s, const ckr_ray *rays, uint32_t n
   return st;
 }
 
+extern "C" int ckr_internal_limit_shadow_queue(ckr_scene *s, uint32_t capacity) {
+  if (!s || capacity == 0) return CKR_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(s->host_mu);
+  s->test_shadow_cap = capacity;
+  return CKR_OK;
+}
+
 extern "C" int ckr_render_stats(ckr_scene *s, uint64_t *closest_rays, uint64_t *shadow_rays, int reset) {
   if (!s || !closest_rays || !shadow_rays) return CKR_ERR_INVALID_ARGUMENT;
   *closest_rays = *shadow_rays = 0;
@@ -520,6 +534,8 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
   P.counts = reinterpret_cast<uint32_t *>(take(32));
   P.stats = reinterpret_cast<unsigned long long *>(take(16));
   P.accum = reinterpret_cast<double *>(take(24ull * kNoAllocMaxPixels));
+  P.sh_cap = kNoAllocShadow;
+  P.status = s->status.ptr;
   // The arena keeps the previous call's contents: clear what must start at zero.
   CKR_CUDA_TRY(cudaMemsetAsync(P.counts, 0, 32, stream));
   CKR_CUDA_TRY(cudaMemsetAsync(P.stats, 0, 16, stream));

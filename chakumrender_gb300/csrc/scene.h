@@ -102,6 +102,9 @@ struct ckr_scene {
   cudaEvent_t pipe_done[kMaxPipes] = {};
   cudaEvent_t user_ready = nullptr;
   int *h_status = nullptr;  // pinned: the status word read back at the end of a host-buffer query
+  // Test hook (ckr_internal_limit_shadow_queue): a shadow-queue capacity for the
+  // next render only; 0 = the size the renderer computes.
+  uint32_t test_shadow_cap = 0;
 };
 
 namespace ckr {

@@ -71,7 +71,20 @@ struct Paths {
                      // k_extend and k_shadow (zeroed before each k_extend)
   unsigned long long *stats;  // cumulative closest-hit rays, shadow rays
   double *accum;     // 3 per output pixel
+  uint32_t sh_cap;   // shadow-queue capacity (rays)
+  int *status;       // the scene's device status word (first CKR_ERR_*)
 };
+
+// Shadow rays of one shading step past the queue's capacity are dropped and the
+// status word records CKR_ERR_QUEUE_OVERFLOW (the host sizes the queue so that
+// this cannot happen; the check keeps a wrong size from writing out of bounds).
+__device__ __forceinline__ uint32_t shadow_fit(const Paths &P, uint32_t sbase, uint32_t nshadow) {
+  if (nshadow && sbase + nshadow > P.sh_cap) {
+    atomicCAS(P.status, 0, CKR_ERR_QUEUE_OVERFLOW);
+    return 0;
+  }
+  return nshadow;
+}
 
 // One job of a batched render: its paths are the global path indices
 // [path_begin, path_begin + npix * spp), its pixels the accumulation rows
@@ -265,7 +278,7 @@ __global__ void __launch_bounds__(TPB, trace_blocks(DYN, TPB)) k_extend(SceneVie
 template <int TPB, bool DYN>
 __global__ void __launch_bounds__(TPB, trace_blocks(DYN, TPB)) k_shadow(SceneView s, Paths P, int depth, int cur, float4 *rec) {
   extern __shared__ uint2 smem_trav[];
-  const uint32_t n = P.counts[2];
+  const uint32_t n = min(P.counts[2], P.sh_cap);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     // Ray statistics: closest-hit rays of this bounce and its shadow rays.
     atomicAdd(&P.stats[0], (unsigned long long)P.counts[cur]);
@@ -560,6 +573,7 @@ __device__ __forceinline__ void shade(ShadeView sv0, Paths P, Params prm, int cu
       nshadow = light_samples<SHADER == CKR_SHADER_DIRECT_MIS>(sv, prm, S, M, fcol, beta, key, meta.y, meta.z, o_off,
                                                                nullptr, nullptr, nullptr, false);
     uint32_t sbase = warp_reserve(&P.counts[2], nshadow);
+    nshadow = shadow_fit(P, sbase, nshadow);
     if (nshadow) {
       if (SHADER == CKR_SHADER_DIRECT_CV) {
         F3 unused = f3(0, 0, 0);
@@ -879,6 +893,7 @@ __global__ void __launch_bounds__(TPB, (1024 / TPB > 1 ? 1024 / TPB : 1))
       }
     }
     uint32_t sbase = warp_reserve(&P.counts[2], nshadow);
+    nshadow = shadow_fit(P, sbase, nshadow);
     if (nshadow) {
       P.sh_o[sbase] = so;
       P.sh_d[sbase] = sd;

@@ -40,6 +40,40 @@ int ckr_internal_ltc_shade_host(const float *gbuf, uint32_t npx, const float *li
  * computed by the tensor-core training kernels without an Adam step. */
 int ckr_internal_proposal_gradients(ckr_proposal *p, const float *rec12, uint32_t n, float *grad, float *loss);
 
+/* Failure paths, driven without a GPU fault.  The next ckr_render on `scene`
+ * runs with a shadow queue of at most `capacity` rays: shading steps that need
+ * more drop their rays and the scene's status word reports
+ * CKR_ERR_QUEUE_OVERFLOW (ckr_scene_check); later renders size the queue
+ * normally. */
+int ckr_internal_limit_shadow_queue(ckr_scene *scene, uint32_t capacity);
+
+/* One inference over n records whose first layer's MMAs are never issued, so
+ * every tile waits on an mbarrier phase that nothing completes; each wait gives
+ * up after `wait_tries` polls, the kernel records CKR_ERR_ITERATION_LIMIT
+ * (ckr_proposal_status) and frees its tensor memory.  The next call runs
+ * normally. */
+int ckr_internal_proposal_infer_stalled(ckr_proposal *p, const float *rec12, uint32_t n, uint16_t *probs,
+                                        uint32_t wait_tries, void *stream);
+
+/* Draws `count` samples from the renderer's device samplers (the functions the
+ * shading kernels call), sample i from the stream (seed, i), into out4 (device,
+ * 16-byte aligned, 4 floats per sample): direction and its density for the
+ * direction samplers, the point and 0 for the triangle.
+ *   CKR_PROBE_BRDF        sample_brdf for material `mat` at normal n, outgoing wo
+ *                         (mirror direction 2(n.wo)n - wo); density pdf_eval
+ *   CKR_PROBE_COSINE      cosine-weighted about n; cos / pi
+ *   CKR_PROBE_HEMISPHERE  uniform on n's hemisphere; 1 / 2 pi
+ *   CKR_PROBE_CONE        uniform in the cone about n with cos(theta_max) = param
+ *   CKR_PROBE_TRIANGLE    uniform point on tri9 (A, B, C) */
+#define CKR_PROBE_BRDF 0
+#define CKR_PROBE_COSINE 1
+#define CKR_PROBE_HEMISPHERE 2
+#define CKR_PROBE_CONE 3
+#define CKR_PROBE_TRIANGLE 4
+int ckr_internal_sample_probe(int kind, const ckr_material *mat, const float n[3], const float wo[3],
+                              const float tri9[9], float param, uint64_t seed, uint32_t count, float *out4,
+                              void *stream);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif

@@ -96,7 +96,7 @@ def test_per_ray_queries_match_oracle_and_batched(torch_cuda, programs, tmp_path
     rays[:, 0:3], rays[:, 4:7], rays[:, 7] = o, d, 1e30
     tri = np.ascontiguousarray(sd.tri9, np.float32).reshape(-1, 9)
     oid, ot = O.OracleBvh(tri).closest(rays)
-    gid = np.where(out["idT"] < 0, 0xFFFFFFFF, out["idT"]).astype(np.uint32)
+    gid = np.where(out["idT"] < 0, 0xFFFFFFFF, out["idT"].astype(np.int64)).astype(np.uint32)
     c = classify(tri, rays, gid, out["tT"].astype(np.float32), oid, ot)
     assert not c["bad"] and c["edge"] + c["tie"] <= 8, c
     hit = out["idT"] >= 0
@@ -108,7 +108,7 @@ def test_per_ray_queries_match_oracle_and_batched(torch_cuda, programs, tmp_path
 
     sph = np.ascontiguousarray(sd.sph4, np.float32).reshape(-1, 4)
     sid, st = O.spheres_closest(sph, rays)
-    got_s = np.where(out["idS"] < 0, 0xFFFFFFFF, out["idS"]).astype(np.uint64)
+    got_s = np.where(out["idS"] < 0, 0xFFFFFFFF, out["idS"].astype(np.int64)).astype(np.uint64)
     assert np.array_equal(got_s, sid.astype(np.uint64))
     hs = out["idS"] >= 0
     assert np.allclose(out["tS"][hs], st[hs], rtol=1e-5)

@@ -262,10 +262,54 @@ def bench_box_render(torch, steps: int):
     sec = a.elapsed_time(b) / 1e3
     closest, shadow = scene.ray_stats(reset=True)
     samples = cam.width * cam.height * cfg.spp * k
+    pixels = cam.width * cam.height * k
+    nbytes = box_state_bytes(samples, closest, shadow, pixels)
+    peak, peak_kind = peaks()
     return {"workload": "box scene 256x256, 16 spp, depth 4, MIS (1 light + 1 BRDF sample), RR 0.3",
             "ms_per_frame": round(1e3 * sec / k, 3), "samples_per_s": round(samples / sec, 1),
             "mrays_per_s": round((closest + shadow) / sec / 1e6, 2),
-            "rays_per_sample": round((closest + shadow) / samples, 3)}
+            "rays_per_sample": round((closest + shadow) / samples, 3),
+            "roofline": {"bound": "hbm", "bytes_per_sample": round(nbytes / samples, 1),
+                         "achieved": round(nbytes / sec / 1e9, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(nbytes / sec / 1e9 / peak, 4), "peak_kind": peak_kind,
+                         "counted": "wavefront state moved between kernels (BOX_STATE_BYTES); the 13-triangle "
+                                    "scene itself stays in L1/L2"}}
+
+
+# Bytes the box render's wavefront stages must move through global memory, from the
+# layout of the path state (csrc/wavefront.cuh): a camera path writes ray_o, ray_d,
+# beta, meta (16 B each) and its queue entry (4 B); a closest-hit ray reads its queue
+# entry and ray (36 B) and writes id + t (8 B); its shading reads queue entry, id,
+# meta, ray, beta, t and the triangle's normal/material word (92 B); a continuation
+# writes the path state and queue entry again (68 B); a shadow ray is written and read
+# once (sh_o, sh_d, sh_c 16 B each + pixel 4 B) and, unoccluded, adds 3 doubles to its
+# pixel (24 B read + 24 B written); per pixel the sums are cleared (24 B), read (24 B)
+# and the image written (12 B).
+BOX_STATE_BYTES = {"camera_path": 68, "closest_ray": 36 + 8 + 92, "continuation": 68, "shadow_ray": 52 + 52 + 48,
+                   "pixel": 24 + 24 + 12}
+
+
+def box_state_bytes(paths, closest, shadow, pixels):
+    B = BOX_STATE_BYTES
+    return (paths * B["camera_path"] + closest * B["closest_ray"] + (closest - paths) * B["continuation"]
+            + shadow * B["shadow_ray"] + pixels * B["pixel"])
+
+
+# FP32 operations of LTC shading per pixel and emitter triangle, counted from the
+# formulas of getLightAnalytic / getLightAnalyticDiffuse (src/lightSources_CV.cpp:221-333)
+# for a triangle wholly above the horizon (a clipped one does more), a fused
+# multiply-add counted as two: specular lobe 3 x (v - x) 9, 3 x Minv v 45, 3
+# normalisations 24, 3 edge integrals (z of the cross product 3, cos 5, clamp 2,
+# (1 - c)(1 + c) 3, theta / sin theta 1) 42, sum 3 -> 126; cosine lobe (v - x) 9, 3
+# normalisations 24, 3 dots with n 15, 3 edge integrals (cross 9, dot with n 5, the
+# same 11, product 1) 78, sum 3 -> 129; radiance weights 12.  Transcendentals (acos,
+# sqrt, rsqrt, divide) per triangle: 30.  Per pixel once: the table lookup and the
+# world-space Minv (about 90).
+LTC_FLOP_PER_PIXEL_TRI = 126 + 129 + 12
+LTC_SFU_PER_PIXEL_TRI = 30
+LTC_FLOP_PER_PIXEL = 90
+# FP32 peak, nominal: 152 SMs x 128 FP32 lanes x 2 (FMA) x 2.07 GHz.
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 
 
 def bench_ltc(torch, steps: int):
@@ -308,8 +352,15 @@ def bench_ltc(torch, steps: int):
     ckr.ltc_mc(g.data_ptr(), n, dt.data_ptr(), dc.data_ptr(), len(lt), 4096, 1, True, mc_f.data_ptr(),
                stream.cuda_stream)
     torch.cuda.synchronize()
+    ntri = lt.reshape(-1, 9).shape[0]
+    flop = n * (LTC_FLOP_PER_PIXEL + ntri * LTC_FLOP_PER_PIXEL_TRI)
     return {"workload": "LTC shading, 1024x1024 G-buffer, 8 quad lights", "ms_per_frame": round(1e3 * sec, 4),
             "mpixels_per_s": round(n / sec / 1e6, 1), "io_gb_per_s": round(n * 60 / sec / 1e9, 1),
+            "roofline": {"bound": "fp32 alu", "flop_per_pixel": LTC_FLOP_PER_PIXEL + ntri * LTC_FLOP_PER_PIXEL_TRI,
+                         "emitter_triangles": ntri, "achieved": round(flop / sec / 1e12, 3),
+                         "peak": round(FP32_PEAK_TFLOPS, 1), "unit": "TFLOP/s",
+                         "frac": round(flop / sec / 1e12 / FP32_PEAK_TFLOPS, 4), "peak_kind": "nominal",
+                         "sfu_per_pixel": ntri * LTC_SFU_PER_PIXEL_TRI},
             "vs_mc_4096spp": {"relmse_ltc_vs_mc": round(rel_mse(ltc, mc), 6),
                               "relmse_ltc_vs_mc_with_fresnel": round(rel_mse(ltc, mc_f), 6),
                               "relmse_mc_seed_to_seed": round(rel_mse(mc2, mc), 7),
@@ -321,11 +372,17 @@ def bench_manylight(torch):
     uniform per triangle in [0.1, 0.8], 10^3 room, 4,096 emissive triangles in 64
     clusters), 1920x1080, 64 spp, max depth 6, one-sample NEE path tracer.  Plain =
     lights chosen in proportion to power; learned = the proposal network (BF16
-    tensor-core MLP, defensive 0.2, Adam 3e-3) trained online from scratch inside
-    the timed frame (cold) or carried over from one earlier frame (warm).  relMSE is
-    taken over a 320x180 window of the frame against a 16,384-spp FP64-accumulated
-    render of that window; the learned frame gets the spp that fit in the plain
-    frame's time."""
+    tensor-core MLP, defensive 0.2, Adam lr 1e-3 as the workload specifies) trained
+    online from scratch inside the timed frame (cold) or carried over from one
+    earlier frame (warm); the learned frame gets the spp that fit in the plain
+    frame's time.
+
+    relMSE is over the whole frame against an FP64-accumulated reference rendered as
+    two independent halves of 1,024 spp: with ref = (h1 + h2) / 2 and the per-pixel
+    estimate (h1 - h2)^2 / 4 of the reference's own variance subtracted,
+    mean(((img - ref)^2 - (h1 - h2)^2 / 4) / (ref^2 + 1e-2)) is an unbiased estimate
+    of the relMSE against the converged image.  The earlier metric (a 320x180 window
+    against 16,384 spp) is reported beside it, as is Adam lr 3e-3."""
     from chakumrender_gb300 import scene as S
     from chakumrender_gb300.proposal import Proposal
 
@@ -341,6 +398,7 @@ def bench_manylight(torch):
         win.pos[k], win.dir[k], win.cx[k], win.cy[k] = cam.pos[k], nd[k], cx[k] * CW / W, cy[k] * CH / H
     win.width, win.height = CW, CH
     rgb = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+    acc = torch.empty((H, W, 3), dtype=torch.float64, device="cuda")
     wrgb = torch.empty((CH, CW, 3), dtype=torch.float32, device="cuda")
 
     def timed(fn):
@@ -352,63 +410,90 @@ def bench_manylight(torch):
 
     cfg = lambda spp, seed: S.render_cfg(shader=S.SHADER_PATH_NEE, spp=spp, max_depth=DEPTH, seed=seed)
     ref_sec = timed(lambda: scene.render(win, cfg(16384, 1000), wrgb.data_ptr()))
-    ref = wrgb.double().cpu().numpy()
+    wref = wrgb.double().cpu().numpy()
+    REF_HALF = 1024
+    halves = []
+    t_ref = 0.0
+    for seed in (2000, 2001):
+        t_ref += timed(lambda: scene.render(cam, cfg(REF_HALF, seed), rgb.data_ptr(), acc.data_ptr()))
+        halves.append(acc.cpu().numpy() / REF_HALF)  # FP64 per-pixel sums
+    fref = 0.5 * (halves[0] + halves[1])
+    fnoise = 0.25 * (halves[0] - halves[1]) ** 2
+    fden = fref * fref + 1e-2
 
     def rel_mse():
-        img = rgb.double().cpu().numpy()[H - Y0 - CH:H - Y0, X0:X0 + CW]
-        return float(np.mean((img - ref) ** 2 / (ref * ref + 1e-2)))
+        img = rgb.double().cpu().numpy()
+        full = float(np.mean(((img - fref) ** 2 - fnoise) / fden))
+        w = img[H - Y0 - CH:H - Y0, X0:X0 + CW]
+        return full, float(np.mean((w - wref) ** 2 / (wref * wref + 1e-2)))
 
     scene.render(cam, cfg(SPP, 1), rgb.data_ptr())  # warm-up
     scene.ray_stats(reset=True)
     t_plain = timed(lambda: scene.render(cam, cfg(SPP, 2), rgb.data_ptr()))
     closest, shadow = scene.ray_stats(reset=True)
     e_plain = rel_mse()
-    opts = dict(minibatch=4096, max_steps=1000, lr=3e-3, batch=262144)
-    cold = Proposal(scene, seed=1, **opts)
-    t_cold64 = timed(lambda: cold.render(cam, cfg(SPP, 3), rgb.data_ptr()))
-    e_cold64 = rel_mse()
-    spp_cold = max(2, int(SPP * t_plain / t_cold64))
-    cold2 = Proposal(scene, seed=2, **opts)
-    t_cold = timed(lambda: cold2.render(cam, cfg(spp_cold, 4), rgb.data_ptr()))
-    e_cold = rel_mse()
-    cold.set_training(False)  # warm: the network of the first learned frame, frozen
-    t_warm64 = timed(lambda: cold.render(cam, cfg(SPP, 5), rgb.data_ptr()))
-    e_warm64 = rel_mse()
-    spp_warm = max(2, int(SPP * t_plain / t_warm64))
-    t_warm = timed(lambda: cold.render(cam, cfg(spp_warm, 6), rgb.data_ptr()))
-    e_warm = rel_mse()
-    st, steps, loss = cold2.status()
-    if st != 0:
-        raise RuntimeError(f"proposal network error {st}")
+
+    def learned_runs(lr):
+        opts = dict(minibatch=4096, max_steps=1000, lr=lr, batch=262144)
+        cold = Proposal(scene, seed=1, **opts)
+        t_c64 = timed(lambda: cold.render(cam, cfg(SPP, 3), rgb.data_ptr()))
+        e_c64 = rel_mse()
+        spp_c = max(2, int(SPP * t_plain / t_c64))
+        cold2 = Proposal(scene, seed=2, **opts)
+        t_c = timed(lambda: cold2.render(cam, cfg(spp_c, 4), rgb.data_ptr()))
+        e_c = rel_mse()
+        st, steps, loss = cold2.status()
+        if st != 0:
+            raise RuntimeError(f"proposal network error {st}")
+        cold.set_training(False)  # warm: the network of the first learned frame, frozen
+        t_w64 = timed(lambda: cold.render(cam, cfg(SPP, 5), rgb.data_ptr()))
+        e_w64 = rel_mse()
+        spp_w = max(2, int(SPP * t_plain / t_w64))
+        t_w = timed(lambda: cold.render(cam, cfg(spp_w, 6), rgb.data_ptr()))
+        e_w = rel_mse()
+        return {"cold_64spp": {"sec": round(t_c64, 4), "relmse": round(e_c64[0], 5),
+                               "relmse_window": round(e_c64[1], 5)},
+                "cold_equal_time": {"spp": spp_c, "sec": round(t_c, 4), "relmse": round(e_c[0], 5),
+                                    "relmse_window": round(e_c[1], 5), "adam_steps": steps,
+                                    "last_loss": round(loss, 4)},
+                "warm_64spp": {"sec": round(t_w64, 4), "relmse": round(e_w64[0], 5),
+                               "relmse_window": round(e_w64[1], 5)},
+                "warm_equal_time": {"spp": spp_w, "sec": round(t_w, 4), "relmse": round(e_w[0], 5),
+                                    "relmse_window": round(e_w[1], 5)},
+                "relmse_ratio_plain_over_learned_equal_time": {
+                    "cold": round(e_plain[0] / e_c[0], 3), "warm": round(e_plain[0] / e_w[0], 3),
+                    "cold_window": round(e_plain[1] / e_c[1], 3), "warm_window": round(e_plain[1] / e_w[1], 3)},
+                "relmse_ratio_plain_over_learned_64spp": {"cold": round(e_plain[0] / e_c64[0], 3),
+                                                          "warm": round(e_plain[0] / e_w64[0], 3)}}
+
+    main_run = learned_runs(1e-3)
+    alt_run = learned_runs(3e-3)
     samples = W * H * SPP
-    return {"workload": "many-light: 1,310,720-tri GGX icosphere in a 10^3 room, 4,096 emitters in 64 clusters, "
-                        "1920x1080, 64 spp, depth 6, one-sample NEE",
-            "plain": {"spp": SPP, "sec": round(t_plain, 4), "relmse": round(e_plain, 5),
-                      "samples_per_s": round(samples / t_plain, 1),
-                      "mrays_per_s": round((closest + shadow) / t_plain / 1e6, 1)},
-            "learned_cold_64spp": {"sec": round(t_cold64, 4), "relmse": round(e_cold64, 5)},
-            "learned_cold_equal_time": {"spp": spp_cold, "sec": round(t_cold, 4), "relmse": round(e_cold, 5),
-                                        "adam_steps": steps, "last_loss": round(loss, 4)},
-            "learned_warm_64spp": {"sec": round(t_warm64, 4), "relmse": round(e_warm64, 5)},
-            "learned_warm_equal_time": {"spp": spp_warm, "sec": round(t_warm, 4), "relmse": round(e_warm, 5)},
-            "relmse_ratio_plain_over_learned_equal_time": {"cold": round(e_plain / e_cold, 3),
-                                                           "warm": round(e_plain / e_warm, 3)},
-            "reference": {"spp": 16384, "window": [X0, Y0, CW, CH], "sec": round(ref_sec, 2),
-                          "accumulation": "fp64"},
-            "proposal": {"minibatch": opts["minibatch"], "batch": opts["batch"], "max_steps": opts["max_steps"],
-                         "defensive": 0.2,
-                         "lr": opts["lr"]}}
+    out = {"workload": "many-light: 1,310,720-tri GGX icosphere in a 10^3 room, 4,096 emitters in 64 clusters, "
+                       "1920x1080, 64 spp, depth 6, one-sample NEE",
+           "plain": {"spp": SPP, "sec": round(t_plain, 4), "relmse": round(e_plain[0], 5),
+                     "relmse_window": round(e_plain[1], 5), "samples_per_s": round(samples / t_plain, 1),
+                     "mrays_per_s": round((closest + shadow) / t_plain / 1e6, 1)},
+           "learned": main_run,
+           "relmse_ratio_plain_over_learned_equal_time": main_run["relmse_ratio_plain_over_learned_equal_time"],
+           "learned_lr_3e-3": alt_run,
+           "reference": {"full_frame": {"spp": 2 * REF_HALF, "halves": 2, "sec": round(t_ref, 2),
+                                        "accumulation": "fp64", "correction": "(h1 - h2)^2 / 4 subtracted"},
+                         "window": {"spp": 16384, "window": [X0, Y0, CW, CH], "sec": round(ref_sec, 2)}},
+           "proposal": {"minibatch": 4096, "batch": 262144, "max_steps": 1000, "defensive": 0.2, "lr": 1e-3}}
+    return out
 
 
 def bench_batch(torch, njobs=64, sizes=(256, 512, 768, 1024), spps=(4, 16, 64)):
     """Box-scene jobs (random sphere BRDFs GGX/Beckmann/Phong with roughness in
     [0.05, 0.9], camera yaw in [-30, 30] degrees, square resolution from `sizes`, spp
-    from `spps`, depth from {3, 6}), path tracer with MIS: one wavefront pass
-    replayed from a CUDA graph (block and wave sizes from the autotuner) against the
-    same jobs rendered one after another with their own launches, and against one
-    ckr_render call per job."""
+    from `spps`, depth from {3, 6}), path tracer with MIS: one pass replayed from a
+    CUDA graph (renderer, block size and paths in flight from the autotuner) against
+    the same jobs rendered one after another with the same renderer (a launch per
+    job), against one ckr_render call per job (the wavefront renderer), and against
+    the whole batch in the wavefront renderer (block 128, 2^21 paths per wave)."""
     from chakumrender_gb300 import scene as S
-    from chakumrender_gb300.batch import Batch, Job, box_jobs
+    from chakumrender_gb300.batch import Batch, BatchTuning, Job, box_jobs
 
     sd = S.load_xml(S.SCENES / "box.xml")
     params, mats = box_jobs(sd, njobs=njobs, seed=4, sizes=sizes, spps=spps)
@@ -447,16 +532,29 @@ def bench_batch(torch, njobs=64, sizes=(256, 512, 768, 1024), spps=(4, 16, 64)):
         ev[3].record(s)
         torch.cuda.synchronize()
     t_api = ev[2].elapsed_time(ev[3]) / 1e3
+    # The same batch in the wavefront renderer, for comparison.
+    bw = Batch(scene, jobs, materials=mats, shader=S.SHADER_PATH, tuning=BatchTuning(128, 1 << 21, 0.0, 0, 0))
+    _, launches_w = bw.stats()
+    bw.render(s.cuda_stream)
+    ev[2].record(s)
+    bw.render(s.cuda_stream)
+    ev[3].record(s)
+    torch.cuda.synchronize()
+    t_wave = ev[2].elapsed_time(ev[3]) / 1e3
+    del bw
     return {"workload": (f"{njobs} box-scene jobs, random sphere BRDFs and yaw, {min(sizes)}^2..{max(sizes)}^2, "
                          f"{'/'.join(map(str, spps))} spp, depth 3/6, path tracer with MIS"),
             "samples": paths, "graph_launches": launches,
             "batched_graph": {"sec": round(t_graph, 4), "samples_per_s": round(paths / t_graph, 1)},
             "sequential_per_job": {"sec": round(t_seq, 4), "samples_per_s": round(paths / t_seq, 1)},
             "one_ckr_render_per_job": {"sec": round(t_api, 4), "samples_per_s": round(paths / t_api, 1)},
+            "wavefront_batch_graph": {"sec": round(t_wave, 4), "samples_per_s": round(paths / t_wave, 1),
+                                      "graph_launches": launches_w},
             "speedup": round(t_seq / t_graph, 3),
             "speedup_vs_ckr_render_per_job": round(t_api / t_graph, 3),
-            "autotuner": {"block": tune.block, "wave": tune.wave, "candidates": tune.candidates,
-                          "reduced_batch_ms": round(tune.ms, 3)},
+            "autotuner": {"renderer": "persistent" if tune.mode == 1 else "wavefront", "block": tune.block,
+                          "paths_in_flight" if tune.mode == 1 else "wave": tune.wave,
+                          "candidates": tune.candidates, "reduced_batch_ms": round(tune.ms, 3)},
             "create_and_capture_s": round(create_s, 2)}
 
 
@@ -608,7 +706,19 @@ def case_box():
     torch.cuda.synchronize()
 
 
-CASES = {"manylight-learned": case_manylight_learned, "manylight-split": case_manylight_split, "trace": case_trace,
+def case_batch():
+    """The batched-jobs workload alone (64 box jobs, and 512 small ones); prints its
+    JSON (for profilers and for tuning the batch renderers)."""
+    import torch
+    from chakumrender_gb300 import build
+
+    build.build_library()
+    out = {"batch": bench_batch(torch), "batch_small": bench_batch(torch, njobs=512, sizes=(32, 48, 64),
+                                                                    spps=(1, 2, 4))}
+    print(json.dumps(out), flush=True)
+
+
+CASES = {"batch": case_batch, "manylight-learned": case_manylight_learned, "manylight-split": case_manylight_split, "trace": case_trace,
          "ltc": case_ltc, "ltc-mc": case_ltc_mc, "box": case_box}
 
 

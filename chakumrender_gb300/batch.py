@@ -21,7 +21,7 @@ class Job(C.Structure):
 
 
 class BatchTuning(C.Structure):
-    _fields_ = [("block", U32), ("wave", U32), ("ms", C.c_float), ("candidates", U32)]
+    _fields_ = [("block", U32), ("wave", U32), ("ms", C.c_float), ("candidates", U32), ("mode", U32)]
 
 
 def _sigs():

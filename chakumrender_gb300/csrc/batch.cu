@@ -1,20 +1,25 @@
 // batch.cu — batched rendering: many jobs of uneven resolution, spp and depth in
-// one wavefront pass, captured as a CUDA graph, with an autotuner for the block
-// size and the wave size.
+// one pass, captured as a CUDA graph, with an autotuner for the renderer, the
+// block size and the number of paths in flight.
 //
 // Paths of all jobs are numbered consecutively (job by job, sample-major inside a
-// job) and processed in waves that cross job boundaries; a path finds its job by
-// binary search over the jobs' first path indices (k_camera) and carries it in
-// meta.w >> 8, so the shading kernels pick the job's materials, seed and depth.
-// The pass is a fixed launch sequence with device-side queue counts, captured
-// once with stream capture and replayed with cudaGraphLaunch.
+// job); a path finds its job by binary search over the jobs' first path indices
+// and carries it in meta.w >> 8, so shading picks the job's materials, seed and
+// depth.  Two renderers:
+//  - persistent (persistent.cuh): one launch of a persistent grid whose lanes
+//    each run a path's whole bounce loop and take the next path of the batch when
+//    theirs ends; the graph is a memset of the sums and the counter, that launch
+//    and the resolve;
+//  - wavefront (wavefront.cuh): waves of paths that cross job boundaries, three
+//    launches per bounce over device-side queues; a fixed launch sequence.
+// The pass is captured once with stream capture and replayed with cudaGraphLaunch.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <vector>
 
+#include "persistent.cuh"
 #include "scene.h"
-#include "wavefront.cuh"
 
 namespace ckr {
 namespace {
@@ -114,6 +119,7 @@ using namespace ckr;
 
 struct ckr_batch {
   ckr_scene *scene = nullptr;
+  DevBuf<unsigned long long> next;  // path counter of the persistent renderer
   uint32_t shader = CKR_SHADER_PATH, n_light = 1;
   float rr_prob = 0.3f;
   uint32_t nmat = 0, nsets = 0;
@@ -124,6 +130,7 @@ struct ckr_batch {
   DevBuf<double> accum;
   ckr_batch_tuning tuning{};
   uint32_t per_path = 1;
+  bool persistent_ok = false;  // shadow rays per vertex fit the persistent kernel's lanes
   uint32_t launches = 0;
   cudaStream_t capture = nullptr;
   cudaGraph_t graph = nullptr;
@@ -211,11 +218,81 @@ int enqueue(ckr_batch *b, JobSet &set, bool pack, size_t wave, cudaStream_t stre
   return CKR_OK;
 }
 
+// The persistent renderer: `lanes` paths in flight (the grid's threads, a
+// multiple of TPB); pack = one launch for the whole batch, else one per job.
+template <int TPB>
+int enqueue_persistent(ckr_batch *b, JobSet &set, bool pack, uint32_t lanes, cudaStream_t stream,
+                       uint32_t *launches) {
+  ckr_scene *s = b->scene;
+  const int depth = (int)stack_depth_of(s);
+  const size_t smem = (size_t)std::max(1, depth) * TPB * sizeof(uint2);
+  const bool nee = b->shader == CKR_SHADER_PATH_NEE;
+  void (*const fn)(SceneView, ShadeView, Params, Paths, uint64_t, uint64_t, unsigned long long *, int) =
+      nee ? k_render_persistent<CKR_SHADER_PATH_NEE, TPB> : k_render_persistent<CKR_SHADER_PATH, TPB>;
+  if (smem > 48 * 1024) CKR_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const uint32_t grid = std::max<uint32_t>(1, lanes / TPB);
+  Params prm{};
+  prm.shader = b->shader;
+  prm.n_light = b->n_light;
+  prm.n_brdf = 1;
+  prm.rr_prob = b->rr_prob;
+  prm.shadow_per_path = b->per_path;
+  prm.jobs = set.dev.ptr;
+  prm.njobs = (uint32_t)set.host.size();
+  prm.spp = 1;
+  prm.npix = 1;
+  SceneView sv = view_of(s);
+  ShadeView shv = shade_view_of(s);
+  shv.mats = b->mats.ptr;
+  Paths P = b->ws.paths(b->accum.ptr);
+  P.status = s->status.ptr;
+  uint32_t n_launch = 0;
+  CKR_CUDA_TRY(cudaMemsetAsync(b->accum.ptr, 0, sizeof(double) * 3 * (size_t)set.pixels, stream));
+  std::vector<std::pair<uint64_t, uint64_t>> ranges;
+  if (pack) ranges.push_back({0, set.paths});
+  else
+    for (const JobDev &J : set.host) ranges.push_back({J.path_begin, (uint64_t)J.npix * J.spp});
+  for (auto [first, count] : ranges) {
+    CKR_CUDA_TRY(cudaMemsetAsync(b->next.ptr, 0, sizeof(unsigned long long), stream));
+    fn<<<grid, TPB, smem, stream>>>(sv, shv, prm, P, first, count, b->next.ptr, depth);
+    ++n_launch;
+  }
+  k_resolve_jobs<<<std::min<unsigned>(2048, ceil_div(set.pixels, 256)), 256, 0, stream>>>(
+      b->accum.ptr, set.dev.ptr, (uint32_t)set.host.size(), set.pixels);
+  ++n_launch;
+  CKR_CUDA_TRY(cudaGetLastError());
+  if (launches) *launches = n_launch;
+  return CKR_OK;
+}
+
 int enqueue_any(ckr_batch *b, JobSet &set, bool pack, const ckr_batch_tuning &t, cudaStream_t stream,
                 uint32_t *launches) {
+  if (t.mode == CKR_BATCH_PERSISTENT) {
+    if (t.block == 64) return enqueue_persistent<64>(b, set, pack, t.wave, stream, launches);
+    if (t.block == 256) return enqueue_persistent<256>(b, set, pack, t.wave, stream, launches);
+    return enqueue_persistent<128>(b, set, pack, t.wave, stream, launches);
+  }
   if (t.block == 64) return enqueue<64>(b, set, pack, t.wave, stream, launches);
   if (t.block == 256) return enqueue<256>(b, set, pack, t.wave, stream, launches);
   return enqueue<128>(b, set, pack, t.wave, stream, launches);
+}
+
+// Resident lanes of the persistent kernel at block size TPB: SMs x resident blocks
+// x TPB.
+template <int TPB>
+uint32_t persistent_lanes(ckr_batch *b) {
+  const int depth = (int)stack_depth_of(b->scene);
+  const size_t smem = (size_t)std::max(1, depth) * TPB * sizeof(uint2);
+  const void *fn = b->shader == CKR_SHADER_PATH_NEE ? (const void *)k_render_persistent<CKR_SHADER_PATH_NEE, TPB>
+                                                     : (const void *)k_render_persistent<CKR_SHADER_PATH, TPB>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return (uint32_t)grid_for(fn, smem, TPB) * TPB;
+}
+
+uint32_t persistent_lanes_of(ckr_batch *b, uint32_t block) {
+  if (block == 64) return persistent_lanes<64>(b);
+  if (block == 256) return persistent_lanes<256>(b);
+  return persistent_lanes<128>(b);
 }
 
 // Times block x wave candidates on the batch with spp capped at 1 (outputs to a
@@ -239,10 +316,40 @@ int autotune(ckr_batch *b, ckr_batch_tuning *best) {
   const uint32_t blocks[3] = {64, 128, 256};
   best->ms = 3.0e38f;
   best->candidates = 0;
+  auto time_one = [&](const ckr_batch_tuning &t) -> int {
+    int r;
+    if ((r = enqueue_any(b, small, true, t, s, nullptr)) != CKR_OK) return r;  // warm-up
+    CKR_CUDA_TRY(cudaEventRecord(e0, s));
+    if ((r = enqueue_any(b, small, true, t, s, nullptr)) != CKR_OK) return r;
+    CKR_CUDA_TRY(cudaEventRecord(e1, s));
+    CKR_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CKR_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    ++best->candidates;
+    if (ms < best->ms) {
+      best->ms = ms;
+      best->block = t.block;
+      best->wave = t.wave;
+      best->mode = t.mode;
+    }
+    return CKR_OK;
+  };
+  // Persistent renderer: the resident grid or half of it, per block size.
+  if (b->persistent_ok) {
+    for (uint32_t blk : blocks) {
+      const uint32_t full = persistent_lanes_of(b, blk);
+      for (uint32_t lanes : {full, std::max(blk, (full / 2) / blk * blk)}) {
+        ckr_batch_tuning t{blk, lanes, 0.f, 0, CKR_BATCH_PERSISTENT};
+        if ((st = time_one(t)) != CKR_OK) break;
+      }
+      if (st != CKR_OK) break;
+    }
+  }
   for (uint32_t blk : blocks) {
+    if (st != CKR_OK) break;
     for (uint32_t w = 1u << 17; w <= (1u << 21); w <<= 1) {
       if (w > 2 * small.paths && w > (1u << 17)) break;
-      ckr_batch_tuning t{blk, w, 0.f, 0};
+      ckr_batch_tuning t{blk, w, 0.f, 0, CKR_BATCH_WAVEFRONT};
       if ((st = b->ws.reserve(w, b->per_path)) != CKR_OK) {
         if (st != CKR_ERR_OUT_OF_MEMORY) break;
         (void)cudaGetLastError();  // the failed allocation's error is not sticky
@@ -250,19 +357,7 @@ int autotune(ckr_batch *b, ckr_batch_tuning *best) {
         st = CKR_OK;
         break;  // next block size
       }
-      if ((st = enqueue_any(b, small, true, t, s, nullptr)) != CKR_OK) break;  // warm-up
-      CKR_CUDA_TRY(cudaEventRecord(e0, s));
-      if ((st = enqueue_any(b, small, true, t, s, nullptr)) != CKR_OK) break;
-      CKR_CUDA_TRY(cudaEventRecord(e1, s));
-      CKR_CUDA_TRY(cudaEventSynchronize(e1));
-      float ms = 0.f;
-      CKR_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
-      ++best->candidates;
-      if (ms < best->ms) {
-        best->ms = ms;
-        best->block = blk;
-        best->wave = w;
-      }
+      if ((st = time_one(t)) != CKR_OK) break;
     }
     if (st != CKR_OK) break;
   }
@@ -318,16 +413,28 @@ extern "C" int ckr_batch_create(ckr_scene *s, uint32_t shader, float rr_prob, ui
   if (st != CKR_OK) return fail(st);
   if (b->accum.reserve(3 * (size_t)b->jobs.pixels) != cudaSuccess) return fail(CKR_ERR_OUT_OF_MEMORY);
   if (cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking) != cudaSuccess) return fail(CKR_ERR_CUDA);
+  if (b->next.reserve(1) != cudaSuccess || b->ws.stats.reserve(2) != cudaSuccess) return fail(CKR_ERR_OUT_OF_MEMORY);
+  if (cudaMemset(b->ws.stats.ptr, 0, 2 * sizeof(unsigned long long)) != cudaSuccess) return fail(CKR_ERR_CUDA);
+  b->persistent_ok = b->per_path <= kInlineShadow;
   std::lock_guard<std::mutex> lock(s->host_mu);
   if (tuning) {
     b->tuning = *tuning;
     if (b->tuning.block != 64 && b->tuning.block != 128 && b->tuning.block != 256) return fail(CKR_ERR_INVALID_ARGUMENT);
-    if (b->tuning.wave < 1024) return fail(CKR_ERR_INVALID_ARGUMENT);
+    if (b->tuning.mode == CKR_BATCH_PERSISTENT) {
+      if (!b->persistent_ok || b->tuning.wave < b->tuning.block) return fail(CKR_ERR_INVALID_ARGUMENT);
+      b->tuning.wave = b->tuning.wave / b->tuning.block * b->tuning.block;
+    } else if (b->tuning.mode != CKR_BATCH_WAVEFRONT || b->tuning.wave < 1024) {
+      return fail(CKR_ERR_INVALID_ARGUMENT);
+    }
   } else if ((st = autotune(b, &b->tuning)) != CKR_OK) {
     return fail(st);
   }
-  b->tuning.wave = (uint32_t)std::min<uint64_t>(b->tuning.wave, std::max<uint64_t>(1024, b->jobs.paths));
-  if ((st = b->ws.reserve(b->tuning.wave, b->per_path)) != CKR_OK) return fail(st);
+  if (b->tuning.mode == CKR_BATCH_WAVEFRONT) {
+    b->tuning.wave = (uint32_t)std::min<uint64_t>(b->tuning.wave, std::max<uint64_t>(1024, b->jobs.paths));
+    if ((st = b->ws.reserve(b->tuning.wave, b->per_path)) != CKR_OK) return fail(st);
+  } else {
+    b->ws.release_waves();  // the autotuner's wavefront candidates
+  }
   if (cudaMemset(b->ws.stats.ptr, 0, 2 * sizeof(unsigned long long)) != cudaSuccess) return fail(CKR_ERR_CUDA);
   // One uncaptured pass first: kernel attributes are set and the kernels loaded
   // outside the capture.

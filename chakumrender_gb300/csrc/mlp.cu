@@ -744,7 +744,7 @@ int pack(Net &net, cudaStream_t stream) {
 namespace {
 template <bool PATHS>
 int launch_infer(const Net &net, const float4 *rec, const PathRows &pr, uint32_t n_max, const uint32_t *n_dev,
-                 __half *probs, uint16_t *cdf16, float delta, cudaStream_t stream) {
+                 __half *probs, uint16_t *cdf16, float delta, cudaStream_t stream, const uint8_t *img = nullptr) {
   if (n_max == 0) return CKR_OK;
   // CTAs resident per SM: shared memory (the opt-in maximum over the CTA's
   // footprint plus the 1 KB the driver reserves per CTA) or 4.
@@ -756,7 +756,7 @@ int launch_infer(const Net &net, const float4 *rec, const PathRows &pr, uint32_t
     per_sm = std::max(1, std::min(4, smem / (int)(sizeof(SmemInfer) + 1024)));
   }
   uint32_t grid = std::min<uint32_t>(ceil_div(n_max, 128 * kGroups), (uint32_t)sm_count() * per_sm);
-  k_mlp_infer<PATHS><<<grid, kInferTPB, sizeof(SmemInfer), stream>>>(rec, pr, n_max, n_dev, 0, net.img,
+  k_mlp_infer<PATHS><<<grid, kInferTPB, sizeof(SmemInfer), stream>>>(rec, pr, n_max, n_dev, 0, img ? img : net.img,
                                                                     params_of(net), delta, probs, cdf16, net.err);
   CKR_CUDA_TRY(cudaGetLastError());
   return CKR_OK;
@@ -769,8 +769,8 @@ int infer(const Net &net, const float4 *rec, uint32_t n_max, const uint32_t *n_d
 }
 
 int infer_paths(const Net &net, const PathRows &rows, uint32_t n_max, const uint32_t *n_dev, uint16_t *cdf16,
-                float delta, cudaStream_t stream) {
-  return launch_infer<true>(net, nullptr, rows, n_max, n_dev, nullptr, cdf16, delta, stream);
+                float delta, cudaStream_t stream, const uint8_t *img) {
+  return launch_infer<true>(net, nullptr, rows, n_max, n_dev, nullptr, cdf16, delta, stream, img);
 }
 
 int gradients(Net &net, const float4 *rec, uint32_t n_max, const uint32_t *n_dev, uint32_t n_off,

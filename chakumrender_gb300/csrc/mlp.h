@@ -62,9 +62,10 @@ void destroy(Net &net);
 // 64 cumulative 16-bit entries per row, pmf(j) = (cdf[j] - cdf[j-1]) / 65535.
 int infer(const Net &net, const float4 *rec, uint32_t n_max, const uint32_t *n_dev, __half *probs, uint16_t *cdf16,
           float delta, cudaStream_t stream);
-// The selection CDFs for the renderer's queue entries [0, min(*n_dev, n_max)).
+// The selection CDFs for the renderer's queue entries [0, min(*n_dev, n_max)), with
+// the weights of `img` (a copy of Net::img; nullptr: Net::img itself).
 int infer_paths(const Net &net, const PathRows &rows, uint32_t n_max, const uint32_t *n_dev, uint16_t *cdf16,
-                float delta, cudaStream_t stream);
+                float delta, cudaStream_t stream, const uint8_t *img = nullptr);
 // One Adam step on the records [0, n) of rec, n = min(*n_dev - n_off, n_max) (rec
 // already advanced by n_off rows) or n_max; skipped (no update) when their weights
 // sum to 0.

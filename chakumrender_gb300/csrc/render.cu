@@ -170,6 +170,11 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
     s->test_shadow_cap = 0;
   }
   bool train = prop && prop->train && (!prop->max_steps || prop->net.step < prop->max_steps);
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  CKR_CUDA_TRY(cudaStreamIsCapturing(stream, &capture));
+  // Training overlaps rendering outside stream capture (see ckr_proposal).
+  const bool overlap = train && capture == cudaStreamCaptureStatusNone;
+  bool pending[2] = {false, false};  // a training whose `done` event the stream has not waited for
   if (prop) {
     CKR_CUDA_TRY(prop->sel[0].reserve(64 * wave));
     CKR_CUDA_TRY(prop->sel[1].reserve(64 * wave));
@@ -179,6 +184,19 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
     P.prev_row = prop->prev_row.ptr;
     P.sh_rec = prop->sh_rec.ptr;
     CKR_CUDA_TRY(cudaMemsetAsync(prop->rec_count.ptr, 0, 4, stream));
+  }
+  if (overlap) {
+    if (!prop->train_stream) CKR_CUDA_TRY(cudaStreamCreateWithFlags(&prop->train_stream, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; ++b) {
+      if (!prop->rec_ready[b]) CKR_CUDA_TRY(cudaEventCreateWithFlags(&prop->rec_ready[b], cudaEventDisableTiming));
+      if (!prop->done[b]) CKR_CUDA_TRY(cudaEventCreateWithFlags(&prop->done[b], cudaEventDisableTiming));
+      CKR_CUDA_TRY(prop->rec_k[b].reserve(3 * (size_t)prop->batch));
+      CKR_CUDA_TRY(prop->rec_count_k[b].reserve(1));
+      CKR_CUDA_TRY(prop->img_pub[b].reserve(mlp::kImgBytes));
+      CKR_CUDA_TRY(cudaMemsetAsync(prop->rec_count_k[b].ptr, 0, 4, stream));
+      CKR_CUDA_TRY(cudaMemcpyAsync(prop->img_pub[b].ptr, prop->net.img, mlp::kImgBytes, cudaMemcpyDeviceToDevice,
+                                   stream));
+    }
   }
   Cam c;
   c.pos = f3(cam->pos[0], cam->pos[1], cam->pos[2]);
@@ -225,6 +243,25 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
     CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), stream));
     Learn lr{};
     if (prop) lr.sel_prev = k ? prop->sel[(k - 1) & 1].ptr : nullptr;
+    // Overlapped training: this step uses record buffer and weight copy b, which the
+    // training of step k - 2 used and wrote; wait for it.  Once training has
+    // stopped, every pending training is waited for and the final weights used.
+    const int b = (int)(k & 1);
+    const uint8_t *img = nullptr;
+    float4 *rec = prop ? prop->rec.ptr : nullptr;
+    uint32_t *rec_count = prop ? prop->rec_count.ptr : nullptr;
+    if (overlap) {
+      for (int i = 0; i < 2; ++i)
+        if (pending[i] && (i == b || !train)) {
+          CKR_CUDA_TRY(cudaStreamWaitEvent(stream, prop->done[i], 0));
+          pending[i] = false;
+        }
+      if (train) {
+        img = prop->img_pub[b].ptr;
+        rec = prop->rec_k[b].ptr;
+        rec_count = prop->rec_count_k[b].ptr;
+      }
+    }
     if (prop && nee) {
       // Light distributions at this step's vertices.
       mlp::PathRows pr;
@@ -236,12 +273,12 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
       pr.meta = P.meta;
       pr.sv = shv;
       int ms = mlp::infer_paths(prop->net, pr, (uint32_t)wave, P.counts + cur, prop->sel[k & 1].ptr,
-                                prop->defensive, stream);
+                                prop->defensive, stream, img);
       if (ms != CKR_OK) return ms;
       lr.sel = prop->sel[k & 1].ptr;
       if (train) {
-        lr.rec = prop->rec.ptr;
-        lr.rec_count = prop->rec_count.ptr;
+        lr.rec = rec;
+        lr.rec_count = rec_count;
         lr.rec_cap = prop->batch;
       }
     }
@@ -258,16 +295,30 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
       k_shade<CKR_SHADER_DIRECT_MIS, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, d, ltc);
     else
       k_shade_miscv<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, d, ltc);
-    shadow_fn<<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur, train && nee ? prop->rec.ptr : nullptr);
+    shadow_fn<<<g_sh, kRTPB, smem, stream>>>(sv, P, depth, cur, train && nee ? rec : nullptr);
     if (train && nee) {
       // Adam steps on this step's light samples (visibility applied above),
       // minibatch by minibatch; steps past the records actually written are no-ops.
+      // Overlapped: on the training stream once the records are complete, then the
+      // new weights are published for step k + 2.
+      cudaStream_t ts_stream = stream;
+      if (overlap) {
+        CKR_CUDA_TRY(cudaEventRecord(prop->rec_ready[b], stream));
+        CKR_CUDA_TRY(cudaStreamWaitEvent(prop->train_stream, prop->rec_ready[b], 0));
+        ts_stream = prop->train_stream;
+      }
       for (uint32_t off = 0; off < prop->batch; off += prop->minibatch) {
-        int ts = mlp::train_step(prop->net, prop->rec.ptr + 3 * (size_t)off,
-                                 std::min(prop->minibatch, prop->batch - off), prop->rec_count.ptr, off, stream);
+        int ts = mlp::train_step(prop->net, rec + 3 * (size_t)off, std::min(prop->minibatch, prop->batch - off),
+                                 rec_count, off, ts_stream);
         if (ts != CKR_OK) return ts;
       }
-      CKR_CUDA_TRY(cudaMemsetAsync(prop->rec_count.ptr, 0, 4, stream));
+      CKR_CUDA_TRY(cudaMemsetAsync(rec_count, 0, 4, ts_stream));
+      if (overlap) {
+        CKR_CUDA_TRY(cudaMemcpyAsync(prop->img_pub[b].ptr, prop->net.img, mlp::kImgBytes, cudaMemcpyDeviceToDevice,
+                                     ts_stream));
+        CKR_CUDA_TRY(cudaEventRecord(prop->done[b], ts_stream));
+        pending[b] = true;
+      }
       if (prop->max_steps && prop->net.step >= prop->max_steps) train = false;  // converged: inference only
     }
     cur ^= 1;
@@ -283,8 +334,6 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   // on shallow trees a step is short and mixing camera rays with bounce rays in
   // one queue costs more than the drained waves' tails (box, 1024^2 x 64 spp:
   // 111 ms against 98 ms with waves), so those keep the waves.
-  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
-  CKR_CUDA_TRY(cudaStreamIsCapturing(stream, &capture));
   const bool regen = (cfg->shader == CKR_SHADER_PATH || cfg->shader == CKR_SHADER_PATH_NEE) && total > wave &&
                      dyn && capture == cudaStreamCaptureStatusNone && total + 64ull * wave < (1ull << 32);
   if (regen) {
@@ -322,6 +371,9 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
       }
     }
   }
+  // The render completes (on `stream`) after its trainings.
+  for (int i = 0; i < 2; ++i)
+    if (pending[i]) CKR_CUDA_TRY(cudaStreamWaitEvent(stream, prop->done[i], 0));
   uint32_t n3 = prm.npix * 3;
   k_resolve<<<std::min<unsigned>(1024, ceil_div(n3, 256)), 256, 0, stream>>>(acc, rgb, n3, 1.0 / prm.spp);
   CKR_CUDA_TRY(cudaGetLastError());

@@ -236,9 +236,11 @@ __device__ __forceinline__ Trav trav_start(const SceneView &s, const RayPre &r) 
 // tests one pending triangle.  The stack lives in shared memory, one column per
 // thread (stack[level * stride]), `depth` entries.  Returns false when the ray is
 // finished (ANY: at its first hit).
-template <bool ANY>
-__device__ __forceinline__ bool trace_step(const SceneView &s, const RayPre &r, float &tbest, uint32_t &best,
-                                           Trav &st, uint2 *stack, int stride, int depth) {
+// `any` is a compile-time constant in the traversal kernels (trace_step<ANY>);
+// the persistent renderer passes it at run time so that one copy of the loop
+// serves its closest-hit and shadow rays.
+__device__ __forceinline__ bool trace_step_rt(const SceneView &s, const RayPre &r, float &tbest, uint32_t &best,
+                                              Trav &st, uint2 *stack, int stride, int depth, const bool ANY) {
   // One exit at the end: early returns for the any-hit case split the warp's
   // control flow and cost more issue slots than the work they skip.
   bool live = true;
@@ -281,10 +283,16 @@ __device__ __forceinline__ bool trace_step(const SceneView &s, const RayPre &r, 
   return live;
 }
 
+template <bool ANY>
+__device__ __forceinline__ bool trace_step(const SceneView &s, const RayPre &r, float &tbest, uint32_t &best,
+                                           Trav &st, uint2 *stack, int stride, int depth) {
+  return trace_step_rt(s, r, tbest, best, st, stack, stride, depth, ANY);
+}
+
 // Spheres of the scene, tested before the triangles.  Returns false when ANY is
 // satisfied by a sphere.
-template <bool ANY>
-__device__ __forceinline__ bool trace_spheres(const SceneView &s, const RayPre &r, float &tbest, uint32_t &best) {
+__device__ __forceinline__ bool trace_spheres_rt(const SceneView &s, const RayPre &r, float &tbest, uint32_t &best,
+                                                 const bool ANY) {
   for (uint32_t k = 0; k < s.nsph; ++k) {
     double t = hit_sphere(r, __ldg(&s.spheres[k]));
     if (t < (double)tbest) {
@@ -294,6 +302,11 @@ __device__ __forceinline__ bool trace_spheres(const SceneView &s, const RayPre &
     }
   }
   return true;
+}
+
+template <bool ANY>
+__device__ __forceinline__ bool trace_spheres(const SceneView &s, const RayPre &r, float &tbest, uint32_t &best) {
+  return trace_spheres_rt(s, r, tbest, best, ANY);
 }
 
 // Traces one ray.  ANY: stop at the first hit.  Returns the hit id (kMiss,
@@ -306,6 +319,18 @@ __device__ __forceinline__ uint32_t trace_ray(const SceneView &s, const RayPre &
   if (!trace_spheres<ANY>(s, r, tbest, best)) return best;
   Trav st = trav_start(s, r);
   while (trace_step<ANY>(s, r, tbest, best, st, stack, stride, depth)) {
+  }
+  return best;
+}
+
+// trace_ray with `any` chosen at run time, not inlined: one copy of the traversal
+// for callers that trace both kinds of ray from one loop (persistent.cuh).
+static __device__ __noinline__ uint32_t trace_ray_rt(const SceneView &s, const RayPre &r, float &tbest, uint2 *stack,
+                                              int stride, int depth, bool any) {
+  uint32_t best = kMiss;
+  if (!trace_spheres_rt(s, r, tbest, best, any)) return best;
+  Trav st = trav_start(s, r);
+  while (trace_step_rt(s, r, tbest, best, st, stack, stride, depth, any)) {
   }
   return best;
 }

@@ -172,18 +172,19 @@ __device__ __forceinline__ void add_px(double *accum, uint32_t px, F3 c) {
   atomicAdd(&accum[3 * (size_t)px + 2], (double)c.z);
 }
 
-// Starts camera path g (path index = sample * npix + pixel, within a job) in path
-// slot `slot`.
-__device__ __forceinline__ void camera_path(const Cam &cam0, const Params &prm, const Paths &P, uint64_t g,
-                                            uint32_t slot) {
+// The state of camera path g (path index = sample * npix + pixel, within a job):
+// ray origin (tmin in w), direction (tmax in w), throughput (MIS weight in w) and
+// meta (output pixel, sample, depth, flags with the job index above bit 8).
+__device__ __forceinline__ void camera_ray(const Cam &cam0, const Params &prm, uint64_t g, float4 &ro, float4 &rd,
+                                           float4 &b4, uint4 &meta) {
+  b4 = make_float4(1.f, 1.f, 1.f, 1.f);
   if (prm.rays) {
     const uint32_t sample = (uint32_t)(g / prm.npix), row = (uint32_t)(g % prm.npix);
     const float4 o = prm.rays[2 * (size_t)row], d4 = prm.rays[2 * (size_t)row + 1];
     const F3 d = normalize(f3(d4.x, d4.y, d4.z));  // shade() takes normalised directions
-    P.ray_o[slot] = make_float4(o.x, o.y, o.z, fmaxf(o.w, 0.f));  // a negative tmin marks explicit rays
-    P.ray_d[slot] = make_float4(d.x, d.y, d.z, d4.w);
-    P.beta[slot] = make_float4(1.f, 1.f, 1.f, 1.f);
-    P.meta[slot] = make_uint4(row, sample, 0u, 0u);
+    ro = make_float4(o.x, o.y, o.z, fmaxf(o.w, 0.f));  // a negative tmin marks explicit rays
+    rd = make_float4(d.x, d.y, d.z, d4.w);
+    meta = make_uint4(row, sample, 0u, 0u);
     return;
   }
   Cam cam = cam0;
@@ -202,11 +203,22 @@ __device__ __forceinline__ void camera_path(const Cam &cam0, const Params &prm, 
   F3 d = cam.cx * (((float)x + jx) / (float)cam.w - 0.5f) + cam.cy * (((float)y + jy) / (float)cam.h - 0.5f) +
          cam.dir;
   d = normalize(d);
-  P.ray_o[slot] = make_float4(cam.pos.x, cam.pos.y, cam.pos.z, 0.f);
-  P.ray_d[slot] = make_float4(d.x, d.y, d.z, 3.0e38f);
-  P.beta[slot] = make_float4(1.f, 1.f, 1.f, 1.f);
+  ro = make_float4(cam.pos.x, cam.pos.y, cam.pos.z, 0.f);
+  rd = make_float4(d.x, d.y, d.z, 3.0e38f);
   uint32_t out_px = (cam.h - 1 - y) * cam.w + x;
-  P.meta[slot] = make_uint4(px_base + out_px, sample, 0u, job << 8);
+  meta = make_uint4(px_base + out_px, sample, 0u, job << 8);
+}
+
+// Starts camera path g in path slot `slot`.
+__device__ __forceinline__ void camera_path(const Cam &cam0, const Params &prm, const Paths &P, uint64_t g,
+                                            uint32_t slot) {
+  float4 ro, rd, b4;
+  uint4 meta;
+  camera_ray(cam0, prm, g, ro, rd, b4, meta);
+  P.ray_o[slot] = ro;
+  P.ray_d[slot] = rd;
+  P.beta[slot] = b4;
+  P.meta[slot] = meta;
 }
 
 // Camera paths wave_base + [0, wave_n) into slots [0, wave_n) and queue 0; the

@@ -303,13 +303,16 @@ int ckr_render_noalloc(ckr_scene *scene, const ckr_camera *cam, const ckr_render
 
 /* ---- batched rendering (no reference counterpart) -------------------------
  * Many jobs of uneven resolution, spp and depth over one scene's geometry are
- * rendered by one wavefront pass: their paths are numbered consecutively and
- * packed into shared waves, so the GPU stays full across job boundaries.  The
- * whole pass (every wave, bounce and resolve) is a fixed launch sequence with no
- * host synchronisation; it is captured once into a CUDA graph and replayed.
- * Each job may use its own material table (same layout as the scene's, e.g.
- * other sphere BRDFs).  Block size and wave size come from an autotuner that
- * times candidates on a reduced copy of the batch (spp capped at 1). */
+ * rendered in one pass: their paths are numbered consecutively, so the GPU stays
+ * full across job boundaries.  Two renderers: PERSISTENT, one launch of a
+ * persistent grid whose lanes each run a path's bounce loop (closest hit,
+ * shading, shadow rays) and take the next path of the batch when theirs ends;
+ * and WAVEFRONT, waves of paths with three launches per bounce over device-side
+ * queues.  The pass (memsets, launches, resolve) has no host synchronisation; it
+ * is captured once into a CUDA graph and replayed.  Each job may use its own
+ * material table (same layout as the scene's, e.g. other sphere BRDFs).  The
+ * renderer, block size and paths in flight come from an autotuner that times
+ * candidates on a reduced copy of the batch (spp capped at 1). */
 typedef struct ckr_job {
   ckr_camera cam;        /* resolution: cam.width x cam.height */
   uint32_t spp, max_depth;
@@ -319,11 +322,16 @@ typedef struct ckr_job {
   float *rgb;            /* device output, width x height x 3 floats, top row first */
 } ckr_job;
 
+#define CKR_BATCH_WAVEFRONT 0
+#define CKR_BATCH_PERSISTENT 1 /* needs <= 4 shadow rays per vertex (lights x samples) */
+
 typedef struct ckr_batch_tuning {
-  uint32_t block;  /* threads per block of the wavefront kernels: 64, 128 or 256 */
-  uint32_t wave;   /* paths per wave (queue capacity), >= 1024 */
+  uint32_t block;  /* threads per block: 64, 128 or 256 */
+  uint32_t wave;   /* WAVEFRONT: paths per wave (queue capacity), >= 1024;
+                      PERSISTENT: paths in flight (the grid's threads) */
   float ms;        /* autotuner: time of the reduced batch with these values */
   uint32_t candidates; /* autotuner: configurations timed */
+  uint32_t mode;   /* CKR_BATCH_WAVEFRONT or CKR_BATCH_PERSISTENT */
 } ckr_batch_tuning;
 
 typedef struct ckr_batch ckr_batch;
@@ -336,8 +344,9 @@ int ckr_batch_create(ckr_scene *scene, uint32_t shader, float rr_prob, uint32_t 
                      const ckr_batch_tuning *tuning, ckr_batch **out);
 /* One replay of the captured graph on `stream` (asynchronous). */
 int ckr_batch_render(ckr_batch *batch, void *stream);
-/* The same jobs one after another, each with its own waves and launches (no
- * packing across jobs, no graph): the baseline the batch is measured against. */
+/* The same jobs one after another with the batch's renderer, each with its own
+ * launches (no packing across jobs, no graph): the baseline the batch is
+ * measured against. */
 int ckr_batch_render_sequential(ckr_batch *batch, void *stream);
 int ckr_batch_get_tuning(const ckr_batch *batch, ckr_batch_tuning *out);
 /* Paths (samples) per replay and launches in the captured graph. */

@@ -718,7 +718,28 @@ def case_batch():
     print(json.dumps(out), flush=True)
 
 
-CASES = {"batch": case_batch, "manylight-learned": case_manylight_learned, "manylight-split": case_manylight_split, "trace": case_trace,
+def case_batch_persistent():
+    """16 box-scene jobs of 256x256 at 4 spp rendered twice by the persistent batch
+    renderer (forced: block 64, 77,824 paths in flight), for profilers."""
+    import torch
+    from chakumrender_gb300 import build
+    from chakumrender_gb300 import scene as S
+    from chakumrender_gb300.batch import Batch, BatchTuning, Job, box_jobs
+
+    build.build_library()
+    sd = S.load_xml(S.SCENES / "box.xml")
+    params, mats = box_jobs(sd, njobs=16, seed=4, sizes=(256,), spps=(4,))
+    outs = [torch.empty((p["cam"].height, p["cam"].width, 3), dtype=torch.float32, device="cuda") for p in params]
+    jobs = [Job(p["cam"], p["spp"], p["max_depth"], p["seed"], p["material_set"], 0, o.data_ptr())
+            for p, o in zip(params, outs)]
+    b = Batch(S.RenderScene(sd), jobs, materials=mats, shader=S.SHADER_PATH,
+              tuning=BatchTuning(64, 77824, 0.0, 0, 1))
+    for _ in range(2):
+        b.render()
+    torch.cuda.synchronize()
+
+
+CASES = {"batch": case_batch, "batch-persistent": case_batch_persistent, "manylight-learned": case_manylight_learned, "manylight-split": case_manylight_split, "trace": case_trace,
          "ltc": case_ltc, "ltc-mc": case_ltc_mc, "box": case_box}
 
 

@@ -186,7 +186,12 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
     CKR_CUDA_TRY(cudaMemsetAsync(prop->rec_count.ptr, 0, 4, stream));
   }
   if (overlap) {
-    if (!prop->train_stream) CKR_CUDA_TRY(cudaStreamCreateWithFlags(&prop->train_stream, cudaStreamNonBlocking));
+    if (!prop->train_stream) {
+      // Highest priority: the training CTAs take SMs as the renderer's blocks retire.
+      int lo = 0, hi = 0;
+      CKR_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+      CKR_CUDA_TRY(cudaStreamCreateWithPriority(&prop->train_stream, cudaStreamNonBlocking, hi));
+    }
     for (int b = 0; b < 2; ++b) {
       if (!prop->rec_ready[b]) CKR_CUDA_TRY(cudaEventCreateWithFlags(&prop->rec_ready[b], cudaEventDisableTiming));
       if (!prop->done[b]) CKR_CUDA_TRY(cudaEventCreateWithFlags(&prop->done[b], cudaEventDisableTiming));

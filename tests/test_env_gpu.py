@@ -34,10 +34,13 @@ def test_box_with_environment_vs_oracle(torch_cuda, shader, spp, nb, depth, ne, 
     e = rel_mse(g, o)
     terms = np.sort(((g - o) ** 2 / (o * o + 1e-2)).ravel())
     trimmed = terms[: int(0.99 * terms.size)].mean()
-    print(f"shader {shader} with environment: relMSE vs oracle {e:.3e}, trimmed {trimmed:.3e}, "
-          f"mean {g.mean():.5f} vs {o.mean():.5f}")
+    o2 = O.render(sd, cam, S.render_cfg(shader=shader, spp=spp, n_light=4, n_brdf=nb, max_depth=depth, seed=7))
+    seed_to_seed = rel_mse(o2, o)
+    print(f"shader {shader} with environment: relMSE vs oracle {e:.3e} (untrimmed), trimmed {trimmed:.3e}, "
+          f"mean {g.mean():.5f} vs {o.mean():.5f}, oracle seed-to-seed relMSE {seed_to_seed:.3e}")
     assert np.all(np.isfinite(g)) and g.min() >= 0
     assert e <= bar and trimmed <= tbar
+    assert e <= 0.1 * seed_to_seed  # divergent paths are a small part of the noise
     assert abs(g.mean() - o.mean()) <= 2e-3 * o.mean()
 
 

@@ -52,7 +52,10 @@ def test_gpu_nee_vs_oracle(torch_cuda, depth):
     grazes an emitter's edge, 1e-3 in front of a wall, hits it in one and misses it
     in the other) that carry a whole emitter's radiance: those pixels are few, so
     the bar is on the fraction of agreeing pixels and on relMSE without the 1%
-    largest per-pixel terms."""
+    largest per-pixel terms.  The untrimmed relMSE is bounded against the noise
+    itself: it must stay a small fraction of the relMSE between two oracle renders
+    with different seeds (a divergent path is another valid sample of the same pixel;
+    an error confined to bright paths would show here and in the means)."""
     sd = small_scene(64, 36, nemit=512, nclusters=64)
     cfg = S.render_cfg(shader=S.SHADER_PATH_NEE, spp=16, max_depth=depth, seed=1)
     scene = S.RenderScene(sd)
@@ -63,9 +66,13 @@ def test_gpu_nee_vs_oracle(torch_cuda, depth):
     agree = np.mean(np.abs(g - o).max(2) <= 1e-3 * np.maximum(1.0, o.max(2)))
     terms = np.sort(((g - o) ** 2 / (o * o + 1e-2)).mean(2).ravel())
     trimmed = terms[: int(0.99 * terms.size)].mean()
-    print(f"PATH_NEE depth {depth}: relMSE {rel_mse(g, o):.3e}, trimmed {trimmed:.3e}, agreeing pixels {agree:.4f}")
+    o2 = O.render(sd, sd.camera, S.render_cfg(shader=S.SHADER_PATH_NEE, spp=16, max_depth=depth, seed=2))
+    seed_to_seed = rel_mse(o2, o)
+    print(f"PATH_NEE depth {depth}: relMSE {rel_mse(g, o):.3e} (untrimmed), trimmed {trimmed:.3e}, agreeing pixels "
+          f"{agree:.4f}, oracle seed-to-seed relMSE {seed_to_seed:.3e}")
     assert agree >= (0.98 if depth == 1 else 0.97)
     assert trimmed <= 1e-4
+    assert rel_mse(g, o) <= 0.1 * seed_to_seed
     if depth == 1:
         assert rel_mse(g, o) <= 1e-3
     assert abs(g.mean() - o.mean()) <= 0.02 * o.mean()

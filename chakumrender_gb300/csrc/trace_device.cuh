@@ -208,8 +208,11 @@ __device__ __forceinline__ void wide_node(const SceneView &s, const RayPre &r, f
     const float tnz = __fmaf_rn(qbyte(nz[h], sh), az, noz), tfz = __fmaf_rn(qbyte(fz[h], sh), az, foz);
     const float en = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
     const float ex = fminf(__fmul_rn(fminf(fminf(tfx, tfy), tfz), kRobustFar), tbest);
-    const uint32_t m = (meta[h] >> sh) & 0xffu;
-    if (en <= ex) hits |= (m >> 5) << (m & 31u);
+    // The slot's hit bits: its pattern (bits 5..7 of the meta byte) shifted to its
+    // position (bits 0..4).  The funnel shift wraps its shift amount, so the bits
+    // above the byte's low five need not be masked off.
+    const uint32_t m = meta[h] >> sh;
+    if (en <= ex) hits |= __funnelshift_l(0u, (m >> 5) & 7u, m);
   }
   ng = make_uint2(__float_as_uint(w1.x), (hits & 0xff000000u) | (ei >> 24));
   tg = make_uint2(__float_as_uint(w1.y), hits & 0x00ffffffu);

@@ -6,7 +6,7 @@
 // specular LTC lobe and the diffuse cosine lobe) and its lanes disagree on the
 // path a triangle takes (above, below or across the horizon), so triangles across
 // the horizon are queued per warp and clipped by all lanes together (k_ltc_shade).
-// CTAs are persistent (two per SM) and stride over pixels; the 64x64 LTC table is
+// CTAs are persistent (three per SM) and stride over pixels; the 64x64 LTC table is
 // read from global memory (two entries per pixel), emitter triangles through the
 // read-only path (every lane of a warp reads the same triangle, a broadcast).
 #include <algorithm>
@@ -20,7 +20,12 @@ namespace ckr {
 namespace {
 
 constexpr int kLtcTPB = 256, kLtcWarps = kLtcTPB / 32;
-constexpr uint32_t kLtcQueue = 512;  // deferred triangles per warp and batch of 32 pixels
+// Deferred triangles per warp and batch of 32 pixels.  256 entries (7.3 KB of shared
+// memory per warp) let three CTAs share an SM: 24 warps at 80 registers with a few
+// spills ran 0.725 ms per 1024^2 frame against 0.846 ms at 512 entries and two CTAs
+// (104 registers); 128 entries at four CTAs (64 registers, 236 bytes of spills) ran
+// 0.966 ms, its queues overflowing into in-place clipping.
+constexpr uint32_t kLtcQueue = 256;
 
 // The clipped integrals for a lane whose warp's queue is full.  Out of line: inlined
 // into the classifying loop they pushed it past 128 registers (60 bytes of spills,
@@ -52,7 +57,7 @@ struct LtcWarp {
 // the few lanes that clip hold up the rest.  Each lane adds its queued terms in a
 // fixed order (newest first), so the result does not depend on scheduling.  A full
 // queue falls back to clipping in place.
-__global__ void __launch_bounds__(kLtcTPB, 2) k_ltc_shade(const float4 *__restrict__ gbuf, uint32_t npx,
+__global__ void __launch_bounds__(kLtcTPB, 3) k_ltc_shade(const float4 *__restrict__ gbuf, uint32_t npx,
                                                        const float *__restrict__ light_tri9,
                                                        const float *__restrict__ light_rgb, uint32_t nlight,
                                                        float *__restrict__ rgb, const LtcEntry *__restrict__ table) {

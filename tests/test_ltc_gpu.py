@@ -60,7 +60,7 @@ def test_full_size_properties(torch_cuda):
 
 def test_many_emitters_fill_the_warp_queues(torch_cuda):
     """96 quads (192 emitter triangles): a warp of 32 pixels meets far more triangles
-    across the horizon than its 512-entry queue holds, so lanes also clip in place
+    across the horizon than its 256-entry queue holds, so lanes also clip in place
     once the queue is full; both routes agree with the oracle, and repeated launches
     give the same bits."""
     g = ckr.gbuffer(91, 4096)

@@ -163,8 +163,9 @@ int enqueue(ckr_batch *b, JobSet &set, bool pack, size_t wave, cudaStream_t stre
   const int g_ext = grid_for((const void *)extend_fn, smem, TPB);
   const int g_sh = grid_for((const void *)shadow_fn, smem, TPB);
   const bool nee = b->shader == CKR_SHADER_PATH_NEE;
-  const int g_shade = grid_for(nee ? (const void *)k_shade_nee<TPB> : (const void *)k_shade_path<TPB>,
-                               0, TPB);
+  void (*const path_fn)(ShadeView, Paths, Params, int, int, const LtcEntry *) =
+      mesh_lights_only(s) ? k_shade_path<TPB, kLightsMeshOnly> : k_shade_path<TPB, kLightsAll>;
+  const int g_shade = grid_for(nee ? (const void *)k_shade_nee<TPB> : (const void *)path_fn, 0, TPB);
   Params prm{};
   prm.shader = b->shader;
   prm.n_light = b->n_light;
@@ -203,7 +204,7 @@ int enqueue(ckr_batch *b, JobSet &set, bool pack, size_t wave, cudaStream_t stre
         CKR_CUDA_TRY(cudaMemsetAsync(P.counts + (cur ^ 1), 0, sizeof(uint32_t), stream));
         CKR_CUDA_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), stream));
         if (nee) k_shade_nee<TPB><<<g_shade, TPB, 0, stream>>>(shv, P, prm, cur, Learn{});
-        else k_shade_path<TPB><<<g_shade, TPB, 0, stream>>>(shv, P, prm, cur, (int)d, nullptr);
+        else path_fn<<<g_shade, TPB, 0, stream>>>(shv, P, prm, cur, (int)d, nullptr);
         shadow_fn<<<g_sh, TPB, smem, stream>>>(sv, P, depth, cur, nullptr);
         n_launch += 3;
         cur ^= 1;
@@ -228,7 +229,9 @@ int enqueue_persistent(ckr_batch *b, JobSet &set, bool pack, uint32_t lanes, cud
   const size_t smem = (size_t)std::max(1, depth) * TPB * sizeof(uint2);
   const bool nee = b->shader == CKR_SHADER_PATH_NEE;
   void (*const fn)(SceneView, ShadeView, Params, Paths, uint64_t, uint64_t, unsigned long long *, int) =
-      nee ? k_render_persistent<CKR_SHADER_PATH_NEE, TPB> : k_render_persistent<CKR_SHADER_PATH, TPB>;
+      nee                    ? k_render_persistent<CKR_SHADER_PATH_NEE, TPB>
+      : mesh_lights_only(s) ? k_render_persistent<CKR_SHADER_PATH, TPB, kLightsMeshOnly>
+                             : k_render_persistent<CKR_SHADER_PATH, TPB, kLightsAll>;
   if (smem > 48 * 1024) CKR_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uint32_t grid = std::max<uint32_t>(1, lanes / TPB);
   Params prm{};
@@ -284,7 +287,8 @@ uint32_t persistent_lanes(ckr_batch *b) {
   const int depth = (int)stack_depth_of(b->scene);
   const size_t smem = (size_t)std::max(1, depth) * TPB * sizeof(uint2);
   const void *fn = b->shader == CKR_SHADER_PATH_NEE ? (const void *)k_render_persistent<CKR_SHADER_PATH_NEE, TPB>
-                                                     : (const void *)k_render_persistent<CKR_SHADER_PATH, TPB>;
+                   : mesh_lights_only(b->scene)      ? (const void *)k_render_persistent<CKR_SHADER_PATH, TPB, kLightsMeshOnly>
+                                                     : (const void *)k_render_persistent<CKR_SHADER_PATH, TPB, kLightsAll>;
   if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   return (uint32_t)grid_for(fn, smem, TPB) * TPB;
 }

@@ -35,6 +35,7 @@ struct LaneShadow {
 // at `t` (the per-lane form of shade<CKR_SHADER_PATH>): emission and environment
 // into the accumulation buffer, the light-technique shadow rays into `sh`, and the
 // continuation in place.  Returns whether the path continues.
+template <uint32_t LF>
 __device__ __noinline__ bool vertex_path(const ShadeView &sv0, const Params &prm, double *accum, uint32_t id,
                                          float t, float4 &ro, float4 &rd, float4 &b4, uint4 &meta,
                                          LaneShadow &sh) {
@@ -43,7 +44,7 @@ __device__ __noinline__ bool vertex_path(const ShadeView &sv0, const Params &prm
   ShadeView sv = sv0;
   sv.mats = sv0.mats + pc.mat_off;
   if (id == kMiss) {
-    if (sv.env_n && meta.z > 0) {
+    if ((LF & kLightEnv) && sv.env_n && meta.z > 0) {
       // A BRDF-sampled ray left the scene: the environment, with its MIS weight.
       const float4 e = env_lookup(sv, f3(rd.x, rd.y, rd.z));
       add_px(accum, meta.x, mulc(f3(b4.x, b4.y, b4.z), f3(e.x, e.y, e.z)) * b4.w);
@@ -70,7 +71,7 @@ __device__ __noinline__ bool vertex_path(const ShadeView &sv0, const Params &prm
   const F3 fcol = f3(mm.color[0], mm.color[1], mm.color[2]) * mm.reflectance;
   const uint64_t key = ckr_key(pc.seed, meta.x - pc.px_base);
   const F3 o_off = offset_origin(S.x, S.n);
-  sh.n = light_samples<false>(sv, prm, S, M, fcol, beta, key, meta.y, meta.z, o_off, sh.o, sh.d, sh.c, true);
+  sh.n = light_samples<false, LF>(sv, prm, S, M, fcol, beta, key, meta.y, meta.z, o_off, sh.o, sh.d, sh.c, true);
   const float e0 = ckr_draw_f(key, ctr(meta.y, meta.z, kDimBrdf));
   const float e1 = ckr_draw_f(key, ctr(meta.y, meta.z, kDimBrdf + 1));
   const float e2 = ckr_draw_f(key, ctr(meta.y, meta.z, kDimBrdf + 2));
@@ -81,7 +82,7 @@ __device__ __noinline__ bool vertex_path(const ShadeView &sv0, const Params &prm
   const float pb = pdf_eval(M, S.n, S.wo_ref, S.wo, w);
   const float f = brdf_eval(M, S.n, S.wo_ref, S.wo, w);
   if (!(pb > 0.f && f > 0.f)) return false;
-  const LightQuery lq = query_lights<true>(sv, S.x, o_off, w, prm.n_light);
+  const LightQuery lq = query_lights<true, LF>(sv, S.x, o_off, w, prm.n_light);
   const float wb = (float)prm.n_brdf * pb / ((float)prm.n_brdf * pb + lq.pdf_sum);
   const F3 nb = mulc(beta, fcol) * (f * c / (pb * (1.0f - prm.rr_prob)));
   ro = make_float4(o_off.x, o_off.y, o_off.z, 0.f);
@@ -199,7 +200,9 @@ constexpr int persist_blocks(int tpb) { return 512 / tpb > 1 ? 512 / tpb : 1; }
 // Renders the batch's paths [first, first + count) (global path indices; `next`
 // counts from 0 and is zeroed before the launch).  Every lane of every warp runs
 // the loop (the refill votes over full warps).
-template <uint32_t SHADER, int TPB>
+// LF: the light kinds compiled into the path vertex (kLightsMeshOnly for scenes whose
+// lights are all MESH / TRI lights).
+template <uint32_t SHADER, int TPB, uint32_t LF = kLightsAll>
 __global__ void __launch_bounds__(TPB, persist_blocks(TPB))
     k_render_persistent(SceneView scene, ShadeView sv, Params prm, Paths P, uint64_t first, uint64_t count,
                         unsigned long long *next, int stack_depth) {
@@ -238,7 +241,7 @@ __global__ void __launch_bounds__(TPB, persist_blocks(TPB))
     ++n_closest;
     const uint32_t px = meta.x;
     active = SHADER == CKR_SHADER_PATH_NEE ? vertex_nee(sv, prm, P.accum, id, t, ro, rd, b4, meta, sh)
-                                           : vertex_path(sv, prm, P.accum, id, t, ro, rd, b4, meta, sh);
+                                           : vertex_path<LF>(sv, prm, P.accum, id, t, ro, rd, b4, meta, sh);
     n_shadow += sh.n;
     for (uint32_t k = 0; k < sh.n; ++k) {
       float ts = sh.d[k].w;

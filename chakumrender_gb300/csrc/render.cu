@@ -228,9 +228,12 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   if (cfg->shader == CKR_SHADER_EXPLICIT && smem > 48 * 1024)
     CKR_CUDA_TRY(cudaFuncSetAttribute(k_shade<CKR_SHADER_EXPLICIT, kRTPB>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // The path shader without the code of light kinds the scene does not have.
+  void (*const path_fn)(ShadeView, Paths, Params, int, int, const LtcEntry *) =
+      mesh_lights_only(s) ? k_shade_path<kRTPB, kLightsMeshOnly> : k_shade_path<kRTPB, kLightsAll>;
   const void *shade_fn = cfg->shader == CKR_SHADER_EXPLICIT ? (const void *)k_shade<CKR_SHADER_EXPLICIT, kRTPB>
                          : cfg->shader == CKR_SHADER_PATH_NEE ? (const void *)k_shade_nee<kRTPB>
-                         : cfg->shader == CKR_SHADER_PATH      ? (const void *)k_shade_path<kRTPB>
+                         : cfg->shader == CKR_SHADER_PATH      ? (const void *)path_fn
                          : cfg->shader == CKR_SHADER_DIRECT_CV  ? (const void *)k_shade<CKR_SHADER_DIRECT_CV, kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_MIS ? (const void *)k_shade<CKR_SHADER_DIRECT_MIS, kRTPB>
                                                                 : (const void *)k_shade_miscv<kRTPB>;
@@ -293,7 +296,7 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
     else if (cfg->shader == CKR_SHADER_PATH_NEE)
       k_shade_nee<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, lr);
     else if (cfg->shader == CKR_SHADER_PATH)
-      k_shade_path<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, d, ltc);
+      path_fn<<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, d, ltc);
     else if (cfg->shader == CKR_SHADER_DIRECT_CV)
       k_shade<CKR_SHADER_DIRECT_CV, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, d, ltc);
     else if (cfg->shader == CKR_SHADER_DIRECT_MIS)
@@ -623,9 +626,12 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
   if (cfg->shader == CKR_SHADER_EXPLICIT && smem > 48 * 1024)
     CKR_CUDA_TRY(cudaFuncSetAttribute(k_shade<CKR_SHADER_EXPLICIT, kRTPB>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // The path shader without the code of light kinds the scene does not have.
+  void (*const path_fn)(ShadeView, Paths, Params, int, int, const LtcEntry *) =
+      mesh_lights_only(s) ? k_shade_path<kRTPB, kLightsMeshOnly> : k_shade_path<kRTPB, kLightsAll>;
   const void *shade_fn = cfg->shader == CKR_SHADER_EXPLICIT ? (const void *)k_shade<CKR_SHADER_EXPLICIT, kRTPB>
                          : cfg->shader == CKR_SHADER_PATH_NEE ? (const void *)k_shade_nee<kRTPB>
-                         : cfg->shader == CKR_SHADER_PATH      ? (const void *)k_shade_path<kRTPB>
+                         : cfg->shader == CKR_SHADER_PATH      ? (const void *)path_fn
                          : cfg->shader == CKR_SHADER_DIRECT_CV  ? (const void *)k_shade<CKR_SHADER_DIRECT_CV, kRTPB>
                          : cfg->shader == CKR_SHADER_DIRECT_MIS ? (const void *)k_shade<CKR_SHADER_DIRECT_MIS, kRTPB>
                                                                 : (const void *)k_shade_miscv<kRTPB>;
@@ -646,7 +652,7 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
       else if (cfg->shader == CKR_SHADER_PATH_NEE)
         k_shade_nee<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, Learn{});
       else if (cfg->shader == CKR_SHADER_PATH)
-        k_shade_path<kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
+        path_fn<<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else if (cfg->shader == CKR_SHADER_DIRECT_CV)
         k_shade<CKR_SHADER_DIRECT_CV, kRTPB><<<g_shade, kRTPB, 0, stream>>>(shv, P, prm, cur, (int)d, ltc);
       else if (cfg->shader == CKR_SHADER_DIRECT_MIS)

@@ -196,9 +196,15 @@ struct LightQuery {
   bool hit;
 };
 
+// Light kinds a shading kernel is compiled for: kernels for scenes whose lights
+// are all MESH / TRI lights leave out the code of the others (a smaller loop body
+// for the instruction caches of the path shader).
+constexpr uint32_t kLightPoint = 1, kLightSphere = 2, kLightEnv = 4;
+constexpr uint32_t kLightsAll = kLightPoint | kLightSphere | kLightEnv, kLightsMeshOnly = 0;
+
 // ENV: the environment light takes part (pdf n_env luminance / A for every
 // direction; seen when no other light is met, src/lightSources.cpp:103-106).
-template <bool ENV = false>
+template <bool ENV = false, uint32_t LF = kLightsAll>
 __device__ __forceinline__ LightQuery query_lights(const ShadeView &sv, F3 x, F3 o_off, F3 w, uint32_t n_per_light) {
   LightQuery q;
   q.pdf_sum = 0.f;
@@ -220,7 +226,7 @@ __device__ __forceinline__ LightQuery query_lights(const ShadeView &sv, F3 x, F3
         q.Le = mat_radiance(sv, sv.tri_mat[id]);
         q.hit = true;
       }
-    } else if (L.type == CKR_LIGHT_SPHERE) {
+    } else if ((LF & kLightSphere) && L.type == CKR_LIGHT_SPHERE) {
       F3 c = f3(L.px, L.py, L.pz);
       F3 wl = c - x;
       float len = length(wl);
@@ -235,7 +241,7 @@ __device__ __forceinline__ LightQuery query_lights(const ShadeView &sv, F3 x, F3
       }
     }
   }
-  if (ENV && sv.env_n) {
+  if (ENV && (LF & kLightEnv) && sv.env_n) {
     const float4 e = env_lookup(sv, w);
     q.pdf_sum += (float)sv.env_n * e.w * sv.env_inv_area;
     if (!q.hit) {
@@ -249,9 +255,10 @@ __device__ __forceinline__ LightQuery query_lights(const ShadeView &sv, F3 x, F3
 
 // One light-technique sample of light L from x (MeshLight::getSamples,
 // getTriLightSurfaceSamples, getSolidDirectionSamples), as a unit direction.
+template <uint32_t LF = kLightsAll>
 __device__ __forceinline__ F3 sample_light(const ShadeView &sv, const DevLight &L, F3 x, float e0, float e1,
                                            float e2) {
-  if (L.type == CKR_LIGHT_SPHERE) {
+  if ((LF & kLightSphere) && L.type == CKR_LIGHT_SPHERE) {
     F3 wl = f3(L.px, L.py, L.pz) - x;
     float len = length(wl);
     float s = L.radius / len;

@@ -320,13 +320,13 @@ __global__ void __launch_bounds__(TPB, trace_blocks(DYN, TPB)) k_shadow(SceneVie
 // Light-technique samples at one surface: returns the number of shadow rays
 // written (one per sample whose direction meets a light), each with its
 // pre-weighted contribution  f * L * cos / sum_k N_k p_k.
-template <bool DETERMINISTIC_SPLIT>
+template <bool DETERMINISTIC_SPLIT, uint32_t LF = kLightsAll>
 __device__ uint32_t light_samples(const ShadeView &sv, const Params &prm, const Surface &S, const Material &M,
                                   F3 fcol, F3 beta, uint64_t key, uint32_t sample, uint32_t depth, F3 o_off,
                                   float4 *so, float4 *sd, float4 *sc, bool write) {
   uint32_t cnt = 0, sidx = 0;
   // Point lights: deterministic, no MIS (src/lightSources.cpp:48-63).
-  for (uint32_t k = sv.first_point; k < sv.nlights; ++k) {
+  for (uint32_t k = sv.first_point; (LF & kLightPoint) && k < sv.nlights; ++k) {
     DevLight L = sv.lights[k];
     F3 dl = f3(L.px, L.py, L.pz) - S.x;
     float dist = length(dl);
@@ -353,10 +353,10 @@ __device__ uint32_t light_samples(const ShadeView &sv, const Params &prm, const 
       float e0 = ckr_draw_f(key, ctr(sample, depth, 3 * sidx));
       float e1 = ckr_draw_f(key, ctr(sample, depth, 3 * sidx + 1));
       float e2 = ckr_draw_f(key, ctr(sample, depth, 3 * sidx + 2));
-      F3 w = sample_light(sv, L, S.x, e0, e1, e2);
+      F3 w = sample_light<LF>(sv, L, S.x, e0, e1, e2);
       float c = dot(w, S.n);
       if (c < 0.f) continue;
-      LightQuery lq = query_lights<true>(sv, S.x, o_off, w, prm.n_light);
+      LightQuery lq = query_lights<true, LF>(sv, S.x, o_off, w, prm.n_light);
       if (!lq.hit) continue;
       if (write) {
         float denom = lq.pdf_sum + (float)prm.n_brdf * pdf_eval(M, S.n, S.wo_ref, S.wo, w);
@@ -371,14 +371,14 @@ __device__ uint32_t light_samples(const ShadeView &sv, const Params &prm, const 
   }
   // Environment light: its own technique after the area lights (EnMpIS of
   // MIS::getSamples, src/mis.cpp:154-166).
-  for (uint32_t i = 0; i < sv.env_n; ++i, ++sidx) {
+  for (uint32_t i = 0; (LF & kLightEnv) && i < sv.env_n; ++i, ++sidx) {
     float e0 = ckr_draw_f(key, ctr(sample, depth, 3 * sidx));
     float e1 = ckr_draw_f(key, ctr(sample, depth, 3 * sidx + 1));
     float e2 = ckr_draw_f(key, ctr(sample, depth, 3 * sidx + 2));
     F3 w = env_sample(sv, e0, e1, e2);
     float c = dot(w, S.n);
     if (c < 0.f) continue;
-    LightQuery lq = query_lights<true>(sv, S.x, o_off, w, prm.n_light);
+    LightQuery lq = query_lights<true, LF>(sv, S.x, o_off, w, prm.n_light);
     if (!lq.hit) continue;
     if (write) {
       float denom = lq.pdf_sum + (float)prm.n_brdf * pdf_eval(M, S.n, S.wo_ref, S.wo, w);
@@ -400,7 +400,7 @@ __device__ uint32_t light_samples(const ShadeView &sv, const Params &prm, const 
       F3 w = i < nlobe ? sample_lobe(M, S.n, S.wo_ref, S.wo, e1, e2) : sample_cosine(S.n, e1, e2);
       float c = dot(w, S.n);
       if (c < 0.f) continue;
-      LightQuery lq = query_lights<true>(sv, S.x, o_off, w, prm.n_light);
+      LightQuery lq = query_lights<true, LF>(sv, S.x, o_off, w, prm.n_light);
       if (!lq.hit) continue;
       if (write) {
         float denom = lq.pdf_sum + (float)nb * pdf_eval(M, S.n, S.wo_ref, S.wo, w);
@@ -498,7 +498,7 @@ __device__ uint32_t cv_samples(const ShadeView &sv, const Params &prm, const Sur
 // of the hemisphere direction at kDimHemi + 2r, + 2r + 1.
 constexpr uint32_t kDimHemi = 1004, kExplicitTries = 8;
 
-template <uint32_t SHADER, int TPB>
+template <uint32_t SHADER, int TPB, uint32_t LF = kLightsAll>
 __device__ __forceinline__ void shade(ShadeView sv0, Paths P, Params prm, int cur, int depth,
                                       const LtcEntry *__restrict__ ltc, SceneView scene, int stack_depth) {
   const uint32_t n = P.counts[cur];
@@ -529,7 +529,7 @@ __device__ __forceinline__ void shade(ShadeView sv0, Paths P, Params prm, int cu
       meta = P.meta[slot];
       pc = path_ctx(prm, meta.w);
       sv.mats = sv0.mats + pc.mat_off;
-      if (id == kMiss && SHADER == CKR_SHADER_PATH && sv.env_n && meta.z > 0) {
+      if ((LF & kLightEnv) && id == kMiss && SHADER == CKR_SHADER_PATH && sv.env_n && meta.z > 0) {
         // A BRDF-sampled ray left the scene: the environment, with its MIS weight.
         const float4 rd = P.ray_d[slot], b4 = P.beta[slot];
         const float4 e = env_lookup(sv, f3(rd.x, rd.y, rd.z));
@@ -582,8 +582,8 @@ __device__ __forceinline__ void shade(ShadeView sv0, Paths P, Params prm, int cu
                                   f3(sv.mats[S.mat].color[0], sv.mats[S.mat].color[1], sv.mats[S.mat].color[2]), key,
                                   meta.y, o_off, cv_neg, nullptr, nullptr, nullptr);
     else if (surface && SHADER != CKR_SHADER_DIRECT_MISCV && SHADER != CKR_SHADER_EXPLICIT)
-      nshadow = light_samples<SHADER == CKR_SHADER_DIRECT_MIS>(sv, prm, S, M, fcol, beta, key, meta.y, meta.z, o_off,
-                                                               nullptr, nullptr, nullptr, false);
+      nshadow = light_samples<SHADER == CKR_SHADER_DIRECT_MIS, LF>(sv, prm, S, M, fcol, beta, key, meta.y, meta.z,
+                                                                   o_off, nullptr, nullptr, nullptr, false);
     uint32_t sbase = warp_reserve(&P.counts[2], nshadow);
     nshadow = shadow_fit(P, sbase, nshadow);
     if (nshadow) {
@@ -593,7 +593,7 @@ __device__ __forceinline__ void shade(ShadeView sv0, Paths P, Params prm, int cu
                          f3(sv.mats[S.mat].color[0], sv.mats[S.mat].color[1], sv.mats[S.mat].color[2]), key, meta.y,
                          o_off, unused, P.sh_o + sbase, P.sh_d + sbase, P.sh_c + sbase);
       } else {
-        light_samples<SHADER == CKR_SHADER_DIRECT_MIS>(sv, prm, S, M, fcol, beta, key, meta.y, meta.z, o_off,
+        light_samples<SHADER == CKR_SHADER_DIRECT_MIS, LF>(sv, prm, S, M, fcol, beta, key, meta.y, meta.z, o_off,
                                                        P.sh_o + sbase, P.sh_d + sbase, P.sh_c + sbase, true);
       }
       for (uint32_t k = 0; k < nshadow; ++k) P.sh_px[sbase + k] = meta.x;
@@ -697,7 +697,7 @@ __device__ __forceinline__ void shade(ShadeView sv0, Paths P, Params prm, int cu
         float pb = pdf_eval(M, S.n, S.wo_ref, S.wo, w);
         float f = brdf_eval(M, S.n, S.wo_ref, S.wo, w);
         if (pb > 0.f && f > 0.f) {
-          LightQuery lq = query_lights<true>(sv, S.x, o_off, w, prm.n_light);
+          LightQuery lq = query_lights<true, LF>(sv, S.x, o_off, w, prm.n_light);
           float wb = (float)prm.n_brdf * pb / ((float)prm.n_brdf * pb + lq.pdf_sum);
           F3 nb = mulc(beta, fcol) * (f * c / (pb * (1.0f - prm.rr_prob)));
           cont = true;
@@ -741,10 +741,21 @@ __global__ void __launch_bounds__(TPB, shade_blocks(SHADER, TPB)) k_shade(ShadeV
   shade<SHADER, TPB>(sv0, P, prm, cur, depth, ltc, scene, stack_depth);
 }
 
-template <int TPB>
+// LF: the light kinds compiled in (kLightsMeshOnly for scenes whose lights are all
+// MESH / TRI lights, see light_kinds_of).
+template <int TPB, uint32_t LF = kLightsAll>
 __global__ void __launch_bounds__(TPB, (640 / TPB > 1 ? 640 / TPB : 1))
     k_shade_path(ShadeView sv0, Paths P, Params prm, int cur, int depth, const LtcEntry *__restrict__ ltc) {
-  shade<CKR_SHADER_PATH, TPB>(sv0, P, prm, cur, depth, ltc, SceneView{}, 0);
+  shade<CKR_SHADER_PATH, TPB, LF>(sv0, P, prm, cur, depth, ltc, SceneView{}, 0);
+}
+
+// Whether a scene's lights are all MESH / TRI lights (no point or sphere light, no
+// environment): its path shader can leave the other kinds' code out.
+inline bool mesh_lights_only(const ckr_scene *s) {
+  if (s->env_n) return false;
+  for (const DevLight &L : s->host_lights)
+    if (L.type != CKR_LIGHT_MESH && L.type != CKR_LIGHT_TRI) return false;
+  return true;
 }
 
 // The reference's default shader (MISCV) at 1024 / TPB resident blocks (64

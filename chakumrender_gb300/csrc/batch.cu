@@ -14,15 +14,21 @@
 //    launches per bounce over device-side queues; a fixed launch sequence.
 // The pass is captured once with stream capture and replayed with cudaGraphLaunch.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstring>
 #include <vector>
 
+#include "ckr_test.h"
 #include "persistent.cuh"
 #include "scene.h"
 
 namespace ckr {
 namespace {
+
+// Test hook (ckr_internal_batch_workspace_cap): wave workspaces larger than this
+// many bytes fail as if device memory had run out; 0 = no cap.
+std::atomic<size_t> g_test_ws_cap{0};
 
 struct BatchWs {
   DevBuf<float4> ray_o, ray_d, beta, sh_o, sh_d, sh_c;
@@ -38,8 +44,13 @@ struct BatchWs {
     q0.release(), q1.release(), sh_o.release(), sh_d.release(), sh_c.release(), sh_px.release();
     wave = shadow = 0;
   }
+  // Bytes of the per-wave buffers for `w` paths: path state 72 B a path (ray_o,
+  // ray_d, beta, meta, hit_id, hit_t, two queue entries), shadow rays 52 B each.
+  static size_t bytes_for(size_t w, size_t per_path) { return 72 * w + 52 * w * per_path; }
   int reserve(size_t w, size_t per_path) {
     size_t sh = w * per_path;
+    const size_t cap = g_test_ws_cap.load();
+    if (cap && bytes_for(w, per_path) > cap) return CKR_ERR_OUT_OF_MEMORY;
     if (ray_o.reserve(w) || ray_d.reserve(w) || beta.reserve(w) || meta.reserve(w) || hit_id.reserve(w) ||
         hit_t.reserve(w) || q0.reserve(w) || q1.reserve(w) || sh_o.reserve(sh) || sh_d.reserve(sh) ||
         sh_c.reserve(sh) || sh_px.reserve(sh) || counts.reserve(8) || stats.reserve(2))
@@ -457,6 +468,11 @@ extern "C" int ckr_batch_create(ckr_scene *s, uint32_t shader, float rr_prob, ui
   b->graph = g;
   if (cudaGraphInstantiate(&b->exec, b->graph, 0) != cudaSuccess) return fail(CKR_ERR_CUDA);
   *out = b;
+  return CKR_OK;
+}
+
+extern "C" int ckr_internal_batch_workspace_cap(uint64_t bytes) {
+  g_test_ws_cap.store((size_t)bytes);
   return CKR_OK;
 }
 

@@ -55,6 +55,12 @@ int ckr_internal_limit_shadow_queue(ckr_scene *scene, uint32_t capacity);
 int ckr_internal_proposal_infer_stalled(ckr_proposal *p, const float *rec12, uint32_t n, uint16_t *probs,
                                         uint32_t wait_tries, void *stream);
 
+/* Batch autotuner under scarce device memory: from now on (process-wide), a
+ * wavefront workspace of more than `bytes` fails as if cudaMalloc had run out
+ * (0 removes the cap).  The autotuner must then keep the best candidate that fits,
+ * and fail with CKR_ERR_OUT_OF_MEMORY only when none does. */
+int ckr_internal_batch_workspace_cap(uint64_t bytes);
+
 /* Draws `count` samples from the renderer's device samplers (the functions the
  * shading kernels call), sample i from the stream (seed, i), into out4 (device,
  * 16-byte aligned, 4 floats per sample): direction and its density for the

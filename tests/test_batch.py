@@ -91,3 +91,46 @@ def test_batch_matches_single_renders(torch_cuda, shader, mode):
             close = np.abs(first[j] - ref).max(2) <= 1e-6 * np.maximum(1.0, np.abs(ref).max(2)) + 1e-7
             rel = float(np.mean((first[j].astype(np.float64) - ref) ** 2 / (ref.astype(np.float64) ** 2 + 1e-2)))
             assert close.mean() >= 0.999 and rel <= 1e-10, (j, close.mean(), rel)
+
+
+@pytest.mark.gpu
+def test_autotuner_under_scarce_memory(torch_cuda):
+    """With device memory too scarce for the larger wave workspaces (simulated by a
+    test cap on the workspace size) the autotuner keeps the best candidate that fits,
+    and the batch still equals the single renders; with room for no candidate at all,
+    creation fails with CKR_ERR_OUT_OF_MEMORY.  Eight light samples per vertex (n_light
+    8) rule out the persistent renderer, so only wavefront candidates compete."""
+    from chakumrender_gb300 import ckr
+    from chakumrender_gb300.batch import Batch
+
+    torch = torch_cuda
+    L = ckr.lib()
+    cap = L.ckr_internal_batch_workspace_cap
+    cap.argtypes = [C.c_uint64]
+    cap.restype = C.c_int
+    sd = S.load_xml(S.SCENES / "box.xml")
+    params, mats, jobs, outs = small_jobs(torch, sd)
+    scene = S.RenderScene(sd)
+    per_path = 8
+    try:
+        assert cap((72 + 52 * per_path) * (1 << 17) + 1) == 0  # room for 2^17-path waves only
+        b = Batch(scene, jobs, materials=mats, shader=S.SHADER_PATH, n_light=per_path)
+        t = b.tuning()
+        assert t.mode == 0 and t.wave <= (1 << 17) and t.candidates > 0
+        b.render()
+        torch.cuda.synchronize()
+        for j, p in enumerate(params):
+            d = S.SceneData(sd.tri9, sd.tri_mat, sd.sph4, sd.sph_mat,
+                            [S.Material.from_buffer_copy(mats[j * sd.nmat + k]) for k in range(sd.nmat)],
+                            [sd.lights[k] for k in range(sd.nlights)])
+            cfg = S.render_cfg(shader=S.SHADER_PATH, spp=p["spp"], max_depth=p["max_depth"], n_light=per_path,
+                               n_brdf=1, rr_prob=0.3, seed=p["seed"])
+            ref = S.RenderScene(d).render_host(p["cam"], cfg)
+            assert np.allclose(outs[j].cpu().numpy(), ref, rtol=1e-6, atol=1e-7), j
+        del b
+        assert cap(1024) == 0  # no wave fits
+        with pytest.raises(ckr.CkrError) as e:
+            Batch(scene, jobs, materials=mats, shader=S.SHADER_PATH, n_light=per_path)
+        assert e.value.status == -3  # CKR_ERR_OUT_OF_MEMORY
+    finally:
+        cap(0)

@@ -13,6 +13,10 @@
 //  - wavefront (wavefront.cuh): waves of paths that cross job boundaries, three
 //    launches per bounce over device-side queues; a fixed launch sequence.
 // The pass is captured once with stream capture and replayed with cudaGraphLaunch.
+// The renderer's traversal kernels run under register caps (launch bounds), where
+// the box test's longer per-node set-up of the byte-permute form spills: they use
+// the conversion form of wide_node (trace_device.cuh).
+#define CKR_WIDE_NODE_CONVERT 1
 #include <algorithm>
 #include <atomic>
 #include <chrono>

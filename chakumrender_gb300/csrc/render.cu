@@ -21,6 +21,10 @@
 //   PATH          the path loop: at every vertex the same MIS estimator with
 //                 n_light_samples per light and one BRDF sample that also
 //                 continues the path; Russian roulette with rr_prob.
+// The renderer's traversal kernels run under register caps (launch bounds), where
+// the box test's longer per-node set-up of the byte-permute form spills: they use
+// the conversion form of wide_node (trace_device.cuh).
+#define CKR_WIDE_NODE_CONVERT 1
 #include <algorithm>
 
 #include "ckr_internal.h"

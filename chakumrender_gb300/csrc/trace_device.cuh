@@ -156,16 +156,21 @@ __device__ __forceinline__ double hit_sphere(const RayPre &r, float4 s) {
 }
 
 // Slack of the quantised slab test, 4 u (u = 2^-24).  The entry distance of a
-// quantised plane p + q 2^e is evaluated as fma(q, 2^e / d, (p - o) / d) with
-// (p - o) / d rounded twice; widening that last term by 4 u of its magnitude
-// (down for the near plane, up for the far one) bounds the rounding so that the
-// computed interval contains the exact one up to the relative factor that
-// kRobustFar absorbs, as in Ize's robust test.
+// quantised plane p + q 2^e is q a + o with a = 2^e / d and o = (p - o_ray) / d,
+// and o is rounded twice; widening o by 4 u of its magnitude (down for the near
+// plane, up for the far one) bounds that rounding so that the computed interval
+// contains the exact one up to the relative factor that kRobustFar absorbs, as in
+// Ize's robust test.
 constexpr float kQuantSlack = 2.384185791015625e-07f;
 
-__device__ __forceinline__ float qbyte(uint32_t w, int shift) { return __uint2float_rn((w >> shift) & 0xffu); }
-
-// Tests the eight child boxes of wide node `node` (layout in bvh_build.h).  Out:
+// Tests the eight child boxes of wide node `node` (layout in bvh_build.h).  Two
+// forms of the same conservative test: by default a plane byte becomes a float
+// through a byte permute folded into the plane's FMA (the traversal kernels: no
+// integer-to-float conversions on the XU pipe, 2.27 -> 2.20 ms per 2^23 rays);
+// with CKR_WIDE_NODE_CONVERT defined by the including file, through an
+// integer-to-float conversion, whose per-node set-up needs fewer registers (the
+// renderer's kernels, register-capped, spill with the first form and ran 5-10 %
+// slower).  Out:
 // ng = (child_base, hit interior children at bits 24 + (slot ^ oct) | imask),
 // tg = (tri_base, hit triangles at their offsets from tri_base).
 __device__ __forceinline__ void wide_node(const SceneView &s, const RayPre &r, float tbest, uint32_t node,
@@ -179,9 +184,28 @@ __device__ __forceinline__ void wide_node(const SceneView &s, const RayPre &r, f
   const float ox = __fmul_rn(__fsub_rn(w0.x, r.ox), r.ix);
   const float oy = __fmul_rn(__fsub_rn(w0.y, r.oy), r.iy);
   const float oz = __fmul_rn(__fsub_rn(w0.z, r.oz), r.iz);
+#ifndef CKR_WIDE_NODE_CONVERT
+  // A plane byte q is read as the float 1 + q 2^-15 (one byte permute puts q in
+  // mantissa bits 8..15 of 1.0f, no integer-to-float conversion), so its distance
+  // q a + o is fma(1 + q 2^-15, 2^15 a, o - 2^15 a).  2^15 a is exact, and
+  // o - 2^15 a is rounded down for near planes and up for far ones, so the FMA's
+  // exact value is never inside q a + o; one rounding follows, as with fma(q, a, o).
+  const float sax = ax * 32768.f, say = ay * 32768.f, saz = az * 32768.f;
+  const float nox = __fsub_rd(__fmaf_rn(-kQuantSlack, fabsf(ox), ox), sax);
+  const float noy = __fsub_rd(__fmaf_rn(-kQuantSlack, fabsf(oy), oy), say);
+  const float noz = __fsub_rd(__fmaf_rn(-kQuantSlack, fabsf(oz), oz), saz);
+  // Far planes also carry kRobustFar, in both FMA operands and rounded up, so that
+  // the exit is min(far planes, tbest) with no multiply per child.
+  const float fax = __fmul_ru(sax, kRobustFar), fay = __fmul_ru(say, kRobustFar), faz = __fmul_ru(saz, kRobustFar);
+  const float fox = __fmul_ru(__fsub_ru(__fmaf_rn(kQuantSlack, fabsf(ox), ox), sax), kRobustFar);
+  const float foy = __fmul_ru(__fsub_ru(__fmaf_rn(kQuantSlack, fabsf(oy), oy), say), kRobustFar);
+  const float foz = __fmul_ru(__fsub_ru(__fmaf_rn(kQuantSlack, fabsf(oz), oz), saz), kRobustFar);
+#else
+  const float sax = ax, say = ay, saz = az, fax = ax, fay = ay, faz = az;
   const float nox = __fmaf_rn(-kQuantSlack, fabsf(ox), ox), fox = __fmaf_rn(kQuantSlack, fabsf(ox), ox);
   const float noy = __fmaf_rn(-kQuantSlack, fabsf(oy), oy), foy = __fmaf_rn(kQuantSlack, fabsf(oy), oy);
   const float noz = __fmaf_rn(-kQuantSlack, fabsf(oz), oz), foz = __fmaf_rn(kQuantSlack, fabsf(oz), oz);
+#endif
   // Near planes are the lo planes on axes the ray travels up, the hi planes otherwise.
   const bool sx = r.ix < 0.f, sy = r.iy < 0.f, sz = r.iz < 0.f;
   const uint32_t lx0 = __float_as_uint(w2.x), lx1 = __float_as_uint(w2.y);
@@ -203,11 +227,22 @@ __device__ __forceinline__ void wide_node(const SceneView &s, const RayPre &r, f
 #pragma unroll
   for (int slot = 0; slot < 8; ++slot) {
     const int h = slot >> 2, sh = (slot & 3) * 8;
-    const float tnx = __fmaf_rn(qbyte(nx[h], sh), ax, nox), tfx = __fmaf_rn(qbyte(fx[h], sh), ax, fox);
-    const float tny = __fmaf_rn(qbyte(ny[h], sh), ay, noy), tfy = __fmaf_rn(qbyte(fy[h], sh), ay, foy);
-    const float tnz = __fmaf_rn(qbyte(nz[h], sh), az, noz), tfz = __fmaf_rn(qbyte(fz[h], sh), az, foz);
+#ifndef CKR_WIDE_NODE_CONVERT
+    const uint32_t sel = 0x7604u | ((uint32_t)(slot & 3) << 4);
+#define QF(w) __uint_as_float(__byte_perm((w), 0x3F800000u, sel))
+#else
+#define QF(w) __uint2float_rn(((w) >> sh) & 0xffu)
+#endif
+    const float tnx = __fmaf_rn(QF(nx[h]), sax, nox), tfx = __fmaf_rn(QF(fx[h]), fax, fox);
+    const float tny = __fmaf_rn(QF(ny[h]), say, noy), tfy = __fmaf_rn(QF(fy[h]), fay, foy);
+    const float tnz = __fmaf_rn(QF(nz[h]), saz, noz), tfz = __fmaf_rn(QF(fz[h]), faz, foz);
+#undef QF
     const float en = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
+#ifndef CKR_WIDE_NODE_CONVERT
+    const float ex = fminf(fminf(tfx, tfy), fminf(tfz, tbest));
+#else
     const float ex = fminf(__fmul_rn(fminf(fminf(tfx, tfy), tfz), kRobustFar), tbest);
+#endif
     // The slot's hit bits: its pattern (bits 5..7 of the meta byte) shifted to its
     // position (bits 0..4).  The funnel shift wraps its shift amount, so the bits
     // above the byte's low five need not be masked off.

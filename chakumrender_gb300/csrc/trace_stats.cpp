@@ -98,15 +98,33 @@ inline float f_of(uint32_t w) {
   return f;
 }
 
+// a - b and a * b rounded down / up, as the device's __fsub_rd / __fsub_ru /
+// __fmul_ru: the round-to-nearest result corrected by the sign of its exact error
+// (TwoSum, and the FMA residual of the product).
+inline float sub_dir(float a, float b, bool up) {
+  const float r = a - b;
+  if (!std::isfinite(r)) return r;
+  const float bb = a - r, err = (a - (r + bb)) + (bb - b);  // a - b = r + err exactly (nb = -b)
+  if (up && err > 0.f) return std::nextafter(r, INFINITY);
+  if (!up && err < 0.f) return std::nextafter(r, -INFINITY);
+  return r;
+}
+inline float mul_up(float a, float b) {
+  const float p = a * b;
+  if (!std::isfinite(p)) return p;
+  return std::fma(a, b, -p) > 0.f ? std::nextafter(p, INFINITY) : p;
+}
+
 // wide_node of trace_device.cuh.
 void wide_node(const uint32_t *w, const Pre &r, float tbest, uint32_t ng[2], uint32_t tg[2]) {
-  float adj[3], on[3], of[3];
+  float sa[3], fa[3], on[3], of[3];
   for (int a = 0; a < 3; ++a) {
     float scale = f_of(((w[3] >> (8 * a)) & 0xffu) << 23);
-    adj[a] = scale * r.inv[a];
+    sa[a] = scale * r.inv[a] * 32768.f;
+    fa[a] = mul_up(sa[a], kRobustFar);
     float o = (f_of(w[a]) - r.o[a]) * r.inv[a];
-    on[a] = std::fma(-kQuantSlack, std::fabs(o), o);
-    of[a] = std::fma(kQuantSlack, std::fabs(o), o);
+    on[a] = sub_dir(std::fma(-kQuantSlack, std::fabs(o), o), sa[a], false);
+    of[a] = mul_up(sub_dir(std::fma(kQuantSlack, std::fabs(o), o), sa[a], true), kRobustFar);
   }
   uint32_t meta[2] = {w[6], w[7]};
   const uint32_t x4 = r.oct * 0x01010101u;
@@ -118,12 +136,14 @@ void wide_node(const uint32_t *w, const Pre &r, float tbest, uint32_t ng[2], uin
     for (int a = 0; a < 3; ++a) {
       const bool neg = r.inv[a] < 0.f;
       const uint32_t lo = w[8 + 4 * a + h], hi = w[10 + 4 * a + h];
-      const float qn = (float)(((neg ? hi : lo) >> sh) & 0xffu), qf = (float)(((neg ? lo : hi) >> sh) & 0xffu);
-      tn[a] = std::fma(qn, adj[a], on[a]);
-      tf[a] = std::fma(qf, adj[a], of[a]);
+      // The byte q as the float 1 + q 2^-15.
+      const float qn = f_of(0x3F800000u | ((((neg ? hi : lo) >> sh) & 0xffu) << 8));
+      const float qf = f_of(0x3F800000u | ((((neg ? lo : hi) >> sh) & 0xffu) << 8));
+      tn[a] = std::fma(qn, sa[a], on[a]);
+      tf[a] = std::fma(qf, fa[a], of[a]);
     }
     const float en = std::fmax(std::fmax(tn[0], tn[1]), std::fmax(tn[2], r.tmin));
-    const float ex = std::fmin(std::fmin(std::fmin(tf[0], tf[1]), tf[2]) * kRobustFar, tbest);
+    const float ex = std::fmin(std::fmin(tf[0], tf[1]), std::fmin(tf[2], tbest));
     const uint32_t m = (meta[h] >> sh) & 0xffu;
     if (en <= ex) hits |= (m >> 5) << (m & 31u);
   }

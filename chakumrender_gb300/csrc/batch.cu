@@ -13,10 +13,6 @@
 //  - wavefront (wavefront.cuh): waves of paths that cross job boundaries, three
 //    launches per bounce over device-side queues; a fixed launch sequence.
 // The pass is captured once with stream capture and replayed with cudaGraphLaunch.
-// The renderer's traversal kernels run under register caps (launch bounds), where
-// the box test's longer per-node set-up of the byte-permute form spills: they use
-// the conversion form of wide_node (trace_device.cuh).
-#define CKR_WIDE_NODE_CONVERT 1
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -165,7 +161,8 @@ template <int TPB>
 int enqueue(ckr_batch *b, JobSet &set, bool pack, size_t wave, cudaStream_t stream, uint32_t *launches) {
   ckr_scene *s = b->scene;
   const int depth = (int)stack_depth_of(s);
-  const size_t smem = (size_t)depth * TPB * sizeof(uint2);
+  size_t smem = (size_t)depth * TPB * sizeof(uint2);
+  smem += shear_smem_bytes(TPB);  // the triangle test's ray data (dynamic fetching)
   // Deep trees: dynamic fetching; one or two levels: one ray per thread.
   const bool dyn = s->max_depth >= kDynamicDepth;
   void (*const extend_fn)(SceneView, Paths, int, int) = dyn ? k_extend<TPB, true> : k_extend<TPB, false>;

@@ -21,10 +21,6 @@
 //   PATH          the path loop: at every vertex the same MIS estimator with
 //                 n_light_samples per light and one BRDF sample that also
 //                 continues the path; Russian roulette with rr_prob.
-// The renderer's traversal kernels run under register caps (launch bounds), where
-// the box test's longer per-node set-up of the byte-permute form spills: they use
-// the conversion form of wide_node (trace_device.cuh).
-#define CKR_WIDE_NODE_CONVERT 1
 #include <algorithm>
 
 #include "ckr_internal.h"
@@ -218,6 +214,7 @@ int render_impl(ckr_scene *s, ckr_proposal *prop, const ckr_camera *cam, const c
   ShadeView shv = shade_view_of(s);
   int depth = (int)stack_depth_of(s);
   size_t smem = (size_t)depth * kRTPB * sizeof(uint2);
+  smem += shear_smem_bytes(kRTPB);  // the triangle test's ray data (dynamic fetching)
   // Deep trees: dynamic fetching; one or two levels: one ray per thread.
   const bool dyn = s->max_depth >= kDynamicDepth;
   void (*const extend_fn)(SceneView, Paths, int, int) = dyn ? k_extend<kRTPB, true> : k_extend<kRTPB, false>;
@@ -616,6 +613,7 @@ extern "C" int ckr_render_noalloc(ckr_scene *s, const ckr_camera *cam, const ckr
   const LtcEntry *ltc = g_noalloc_ltc_dev[dev];
   int depth = (int)stack_depth_of(s);
   size_t smem = (size_t)depth * kRTPB * sizeof(uint2);
+  smem += shear_smem_bytes(kRTPB);  // the triangle test's ray data (dynamic fetching)
   // Deep trees: dynamic fetching; one or two levels: one ray per thread.
   const bool dyn = s->max_depth >= kDynamicDepth;
   void (*const extend_fn)(SceneView, Paths, int, int) = dyn ? k_extend<kRTPB, true> : k_extend<kRTPB, false>;

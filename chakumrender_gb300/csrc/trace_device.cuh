@@ -83,17 +83,32 @@ __device__ __forceinline__ RayPre make_ray(float4 a, float4 b) {
 // Watertight test of one triangle; on a hit inside (tmin, tbest) stores t and
 // returns true.  Also applies the reference's near-parallel rejection
 // (d.n)^2 <= 1e-10 with n the unit normal (src/geometryPrimitives.cpp:43).
+// What the triangle test reads of a ray besides its origin and tmin: the shear rows
+// and the direction (RayPre::m*, d*), for callers that keep them outside RayPre.
+struct Shear {
+  float mx0, mx1, mx2, my0, my1, my2, mz0, mz1, mz2, dx, dy, dz;
+};
+
+__device__ __forceinline__ bool hit_triangle_sheared(const RayPre &r, const Shear &m, float4 v0, float4 v1,
+                                                     float4 v2, float tbest, float &t_out);
+
 __device__ __forceinline__ bool hit_triangle(const RayPre &r, float4 v0, float4 v1, float4 v2,
                                              float tbest, float &t_out) {
+  const Shear m{r.mx0, r.mx1, r.mx2, r.my0, r.my1, r.my2, r.mz0, r.mz1, r.mz2, r.dx, r.dy, r.dz};
+  return hit_triangle_sheared(r, m, v0, v1, v2, tbest, t_out);
+}
+
+__device__ __forceinline__ bool hit_triangle_sheared(const RayPre &r, const Shear &m, float4 v0, float4 v1,
+                                                     float4 v2, float tbest, float &t_out) {
   float a0 = v0.x - r.ox, a1 = v0.y - r.oy, a2 = v0.z - r.oz;
   float b0 = v1.x - r.ox, b1 = v1.y - r.oy, b2 = v1.z - r.oz;
   float c0 = v2.x - r.ox, c1 = v2.y - r.oy, c2 = v2.z - r.oz;
-  float Ax = fmaf(r.mx0, a0, fmaf(r.mx1, a1, r.mx2 * a2));
-  float Ay = fmaf(r.my0, a0, fmaf(r.my1, a1, r.my2 * a2));
-  float Bx = fmaf(r.mx0, b0, fmaf(r.mx1, b1, r.mx2 * b2));
-  float By = fmaf(r.my0, b0, fmaf(r.my1, b1, r.my2 * b2));
-  float Cx = fmaf(r.mx0, c0, fmaf(r.mx1, c1, r.mx2 * c2));
-  float Cy = fmaf(r.my0, c0, fmaf(r.my1, c1, r.my2 * c2));
+  float Ax = fmaf(m.mx0, a0, fmaf(m.mx1, a1, m.mx2 * a2));
+  float Ay = fmaf(m.my0, a0, fmaf(m.my1, a1, m.my2 * a2));
+  float Bx = fmaf(m.mx0, b0, fmaf(m.mx1, b1, m.mx2 * b2));
+  float By = fmaf(m.my0, b0, fmaf(m.my1, b1, m.my2 * b2));
+  float Cx = fmaf(m.mx0, c0, fmaf(m.mx1, c1, m.mx2 * c2));
+  float Cy = fmaf(m.my0, c0, fmaf(m.my1, c1, m.my2 * c2));
   float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
   float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
   float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
@@ -106,9 +121,9 @@ __device__ __forceinline__ bool hit_triangle(const RayPre &r, float4 v0, float4 
   if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return false;
   float det = U + V + W;
   if (det == 0.f) return false;
-  float Az = fmaf(r.mz0, a0, fmaf(r.mz1, a1, r.mz2 * a2));
-  float Bz = fmaf(r.mz0, b0, fmaf(r.mz1, b1, r.mz2 * b2));
-  float Cz = fmaf(r.mz0, c0, fmaf(r.mz1, c1, r.mz2 * c2));
+  float Az = fmaf(m.mz0, a0, fmaf(m.mz1, a1, m.mz2 * a2));
+  float Bz = fmaf(m.mz0, b0, fmaf(m.mz1, b1, m.mz2 * b2));
+  float Cz = fmaf(m.mz0, c0, fmaf(m.mz1, c1, m.mz2 * c2));
   float T = fmaf(U, Az, fmaf(V, Bz, W * Cz));
   float t = __fdiv_rn(T, det);
   if (!(t > r.tmin) || !(t < tbest)) return false;
@@ -116,7 +131,7 @@ __device__ __forceinline__ bool hit_triangle(const RayPre &r, float4 v0, float4 
   float e10 = v1.x - v0.x, e11 = v1.y - v0.y, e12 = v1.z - v0.z;
   float e20 = v2.x - v0.x, e21 = v2.y - v0.y, e22 = v2.z - v0.z;
   float n0 = e21 * e12 - e22 * e11, n1 = e22 * e10 - e20 * e12, n2 = e20 * e11 - e21 * e10;
-  float dn = r.dx * n0 + r.dy * n1 + r.dz * n2;
+  float dn = m.dx * n0 + m.dy * n1 + m.dz * n2;
   if (dn * dn <= 1e-10f * (n0 * n0 + n1 * n1 + n2 * n2)) return false;
   t_out = t;
   return true;
@@ -164,15 +179,15 @@ __device__ __forceinline__ double hit_sphere(const RayPre &r, float4 s) {
 constexpr float kQuantSlack = 2.384185791015625e-07f;
 
 // Tests the eight child boxes of wide node `node` (layout in bvh_build.h).  Two
-// forms of the same conservative test: by default a plane byte becomes a float
-// through a byte permute folded into the plane's FMA (the traversal kernels: no
-// integer-to-float conversions on the XU pipe, 2.27 -> 2.20 ms per 2^23 rays);
-// with CKR_WIDE_NODE_CONVERT defined by the including file, through an
-// integer-to-float conversion, whose per-node set-up needs fewer registers (the
-// renderer's kernels, register-capped, spill with the first form and ran 5-10 %
-// slower).  Out:
+// forms of the same conservative test: PERMUTE, a plane byte becomes a float
+// through a byte permute folded into the plane's FMA (no integer-to-float
+// conversions on the XU pipe: the traversal kernels, 2.27 -> 2.20 ms per 2^23
+// rays); otherwise through an integer-to-float conversion, whose per-node set-up
+// needs fewer registers (the renderer's one-ray-per-thread kernels, capped at 64
+// registers, spill with the first form and ran 5-10 % slower).  Out:
 // ng = (child_base, hit interior children at bits 24 + (slot ^ oct) | imask),
 // tg = (tri_base, hit triangles at their offsets from tri_base).
+template <bool PERMUTE>
 __device__ __forceinline__ void wide_node(const SceneView &s, const RayPre &r, float tbest, uint32_t node,
                                           uint2 &ng, uint2 &tg) {
   const float4 *np = s.nodes + 5 * (size_t)node;
@@ -184,28 +199,38 @@ __device__ __forceinline__ void wide_node(const SceneView &s, const RayPre &r, f
   const float ox = __fmul_rn(__fsub_rn(w0.x, r.ox), r.ix);
   const float oy = __fmul_rn(__fsub_rn(w0.y, r.oy), r.iy);
   const float oz = __fmul_rn(__fsub_rn(w0.z, r.oz), r.iz);
-#ifndef CKR_WIDE_NODE_CONVERT
-  // A plane byte q is read as the float 1 + q 2^-15 (one byte permute puts q in
-  // mantissa bits 8..15 of 1.0f, no integer-to-float conversion), so its distance
-  // q a + o is fma(1 + q 2^-15, 2^15 a, o - 2^15 a).  2^15 a is exact, and
-  // o - 2^15 a is rounded down for near planes and up for far ones, so the FMA's
-  // exact value is never inside q a + o; one rounding follows, as with fma(q, a, o).
-  const float sax = ax * 32768.f, say = ay * 32768.f, saz = az * 32768.f;
-  const float nox = __fsub_rd(__fmaf_rn(-kQuantSlack, fabsf(ox), ox), sax);
-  const float noy = __fsub_rd(__fmaf_rn(-kQuantSlack, fabsf(oy), oy), say);
-  const float noz = __fsub_rd(__fmaf_rn(-kQuantSlack, fabsf(oz), oz), saz);
-  // Far planes also carry kRobustFar, in both FMA operands and rounded up, so that
-  // the exit is min(far planes, tbest) with no multiply per child.
-  const float fax = __fmul_ru(sax, kRobustFar), fay = __fmul_ru(say, kRobustFar), faz = __fmul_ru(saz, kRobustFar);
-  const float fox = __fmul_ru(__fsub_ru(__fmaf_rn(kQuantSlack, fabsf(ox), ox), sax), kRobustFar);
-  const float foy = __fmul_ru(__fsub_ru(__fmaf_rn(kQuantSlack, fabsf(oy), oy), say), kRobustFar);
-  const float foz = __fmul_ru(__fsub_ru(__fmaf_rn(kQuantSlack, fabsf(oz), oz), saz), kRobustFar);
-#else
-  const float sax = ax, say = ay, saz = az, fax = ax, fay = ay, faz = az;
-  const float nox = __fmaf_rn(-kQuantSlack, fabsf(ox), ox), fox = __fmaf_rn(kQuantSlack, fabsf(ox), ox);
-  const float noy = __fmaf_rn(-kQuantSlack, fabsf(oy), oy), foy = __fmaf_rn(kQuantSlack, fabsf(oy), oy);
-  const float noz = __fmaf_rn(-kQuantSlack, fabsf(oz), oz), foz = __fmaf_rn(kQuantSlack, fabsf(oz), oz);
-#endif
+  float sax, say, saz, fax, fay, faz, nox, noy, noz, fox, foy, foz;
+  if constexpr (PERMUTE) {
+    // A plane byte q is read as the float 1 + q 2^-15 (one byte permute puts q in
+    // mantissa bits 8..15 of 1.0f, no integer-to-float conversion), so its distance
+    // q a + o is fma(1 + q 2^-15, 2^15 a, o - 2^15 a).  2^15 a is exact, and
+    // o - 2^15 a is rounded down for near planes and up for far ones, so the FMA's
+    // exact value is never inside q a + o; one rounding follows, as with fma(q, a, o).
+    sax = ax * 32768.f;
+    say = ay * 32768.f;
+    saz = az * 32768.f;
+    nox = __fsub_rd(__fmaf_rn(-kQuantSlack, fabsf(ox), ox), sax);
+    noy = __fsub_rd(__fmaf_rn(-kQuantSlack, fabsf(oy), oy), say);
+    noz = __fsub_rd(__fmaf_rn(-kQuantSlack, fabsf(oz), oz), saz);
+    // Far planes also carry kRobustFar, in both FMA operands and rounded up, so that
+    // the exit is min(far planes, tbest) with no multiply per child.
+    fax = __fmul_ru(sax, kRobustFar);
+    fay = __fmul_ru(say, kRobustFar);
+    faz = __fmul_ru(saz, kRobustFar);
+    fox = __fmul_ru(__fsub_ru(__fmaf_rn(kQuantSlack, fabsf(ox), ox), sax), kRobustFar);
+    foy = __fmul_ru(__fsub_ru(__fmaf_rn(kQuantSlack, fabsf(oy), oy), say), kRobustFar);
+    foz = __fmul_ru(__fsub_ru(__fmaf_rn(kQuantSlack, fabsf(oz), oz), saz), kRobustFar);
+  } else {
+    sax = fax = ax;
+    say = fay = ay;
+    saz = faz = az;
+    nox = __fmaf_rn(-kQuantSlack, fabsf(ox), ox);
+    fox = __fmaf_rn(kQuantSlack, fabsf(ox), ox);
+    noy = __fmaf_rn(-kQuantSlack, fabsf(oy), oy);
+    foy = __fmaf_rn(kQuantSlack, fabsf(oy), oy);
+    noz = __fmaf_rn(-kQuantSlack, fabsf(oz), oz);
+    foz = __fmaf_rn(kQuantSlack, fabsf(oz), oz);
+  }
   // Near planes are the lo planes on axes the ray travels up, the hi planes otherwise.
   const bool sx = r.ix < 0.f, sy = r.iy < 0.f, sz = r.iz < 0.f;
   const uint32_t lx0 = __float_as_uint(w2.x), lx1 = __float_as_uint(w2.y);
@@ -227,22 +252,17 @@ __device__ __forceinline__ void wide_node(const SceneView &s, const RayPre &r, f
 #pragma unroll
   for (int slot = 0; slot < 8; ++slot) {
     const int h = slot >> 2, sh = (slot & 3) * 8;
-#ifndef CKR_WIDE_NODE_CONVERT
+    // The plane byte of this slot as the FMA's first operand.
     const uint32_t sel = 0x7604u | ((uint32_t)(slot & 3) << 4);
-#define QF(w) __uint_as_float(__byte_perm((w), 0x3F800000u, sel))
-#else
-#define QF(w) __uint2float_rn(((w) >> sh) & 0xffu)
-#endif
-    const float tnx = __fmaf_rn(QF(nx[h]), sax, nox), tfx = __fmaf_rn(QF(fx[h]), fax, fox);
-    const float tny = __fmaf_rn(QF(ny[h]), say, noy), tfy = __fmaf_rn(QF(fy[h]), fay, foy);
-    const float tnz = __fmaf_rn(QF(nz[h]), saz, noz), tfz = __fmaf_rn(QF(fz[h]), faz, foz);
-#undef QF
+    auto qf = [&](uint32_t w) {
+      return PERMUTE ? __uint_as_float(__byte_perm(w, 0x3F800000u, sel)) : __uint2float_rn((w >> sh) & 0xffu);
+    };
+    const float tnx = __fmaf_rn(qf(nx[h]), sax, nox), tfx = __fmaf_rn(qf(fx[h]), fax, fox);
+    const float tny = __fmaf_rn(qf(ny[h]), say, noy), tfy = __fmaf_rn(qf(fy[h]), fay, foy);
+    const float tnz = __fmaf_rn(qf(nz[h]), saz, noz), tfz = __fmaf_rn(qf(fz[h]), faz, foz);
     const float en = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
-#ifndef CKR_WIDE_NODE_CONVERT
-    const float ex = fminf(fminf(tfx, tfy), fminf(tfz, tbest));
-#else
-    const float ex = fminf(__fmul_rn(fminf(fminf(tfx, tfy), tfz), kRobustFar), tbest);
-#endif
+    const float ex = PERMUTE ? fminf(fminf(tfx, tfy), fminf(tfz, tbest))
+                             : fminf(__fmul_rn(fminf(fminf(tfx, tfy), tfz), kRobustFar), tbest);
     // The slot's hit bits: its pattern (bits 5..7 of the meta byte) shifted to its
     // position (bits 0..4).  The funnel shift wraps its shift amount, so the bits
     // above the byte's low five need not be masked off.
@@ -277,8 +297,21 @@ __device__ __forceinline__ Trav trav_start(const SceneView &s, const RayPre &r) 
 // `any` is a compile-time constant in the traversal kernels (trace_step<ANY>);
 // the persistent renderer passes it at run time so that one copy of the loop
 // serves its closest-hit and shadow rays.
+// The traversal policy of trace_step: where the triangle test reads the ray's shear
+// rows and direction (by default the ray's own registers; TriShearSmem reads them
+// from shared memory) and which form of the box test wide_node uses.
+struct TriInRegs {
+  static constexpr bool kPermutePlanes = false;
+  __device__ __forceinline__ bool operator()(const RayPre &r, float4 v0, float4 v1, float4 v2, float tbest,
+                                             float &t) const {
+    return hit_triangle(r, v0, v1, v2, tbest, t);
+  }
+};
+
+template <class Tri = TriInRegs>
 __device__ __forceinline__ bool trace_step_rt(const SceneView &s, const RayPre &r, float &tbest, uint32_t &best,
-                                              Trav &st, uint2 *stack, int stride, int depth, const bool ANY) {
+                                              Trav &st, uint2 *stack, int stride, int depth, const bool ANY,
+                                              Tri tri = Tri{}) {
   // One exit at the end: early returns for the any-hit case split the warp's
   // control flow and cost more issue slots than the work they skip.
   bool live = true;
@@ -303,7 +336,7 @@ __device__ __forceinline__ bool trace_step_rt(const SceneView &s, const RayPre &
           live = false;
         }
       }
-      if (live) wide_node(s, r, tbest, child, st.ng, st.tg);
+      if (live) wide_node<Tri::kPermutePlanes>(s, r, tbest, child, st.ng, st.tg);
     }
   }
   if (live && st.tg.y != 0) {
@@ -312,7 +345,7 @@ __device__ __forceinline__ bool trace_step_rt(const SceneView &s, const RayPre &
     const float4 *tp = s.tris + 3 * (size_t)(st.tg.x + k);
     const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
     float t;
-    if (hit_triangle(r, v0, v1, v2, tbest, t)) {
+    if (tri(r, v0, v1, v2, tbest, t)) {
       tbest = t;
       best = __float_as_uint(v0.w);
       if (ANY) live = false;
@@ -321,10 +354,10 @@ __device__ __forceinline__ bool trace_step_rt(const SceneView &s, const RayPre &
   return live;
 }
 
-template <bool ANY>
+template <bool ANY, class Tri = TriInRegs>
 __device__ __forceinline__ bool trace_step(const SceneView &s, const RayPre &r, float &tbest, uint32_t &best,
-                                           Trav &st, uint2 *stack, int stride, int depth) {
-  return trace_step_rt(s, r, tbest, best, st, stack, stride, depth, ANY);
+                                           Trav &st, uint2 *stack, int stride, int depth, Tri tri = Tri{}) {
+  return trace_step_rt(s, r, tbest, best, st, stack, stride, depth, ANY, tri);
 }
 
 // Spheres of the scene, tested before the triangles.  Returns false when ANY is
@@ -387,9 +420,41 @@ constexpr int kRefill = 8;
 // here (the loop votes over full warps).
 //   fetch(i, r, tbest) -> bool: sets up work item i < n (ray, tmax); false skips it.
 //   finish(i, best, tbest): stores the result of item i.
-template <bool ANY, class Fetch, class Finish>
+// The triangle test's ray data (shear rows and direction, Shear) kept in shared
+// memory instead of registers: three float4 per thread in a column of stride TPB
+// after the traversal stacks (depth x TPB uint2), written once per ray by the
+// kernel's fetch and read back by the triangle test (2.5 tests per ray against 11
+// node visits on the 1.3M-triangle mesh).  Frees twelve registers across the
+// traversal loop.
+constexpr size_t shear_smem_bytes(int tpb) { return 3 * (size_t)tpb * sizeof(float4); }
+
+template <int TPB>
+__device__ __forceinline__ float4 *shear_column(uint2 *smem_stacks, int depth) {
+  return reinterpret_cast<float4 *>(smem_stacks + (size_t)depth * TPB) + threadIdx.x;
+}
+
+template <int TPB>
+__device__ __forceinline__ void store_shear(float4 *col, const RayPre &r) {
+  col[0] = make_float4(r.mx0, r.mx1, r.mx2, r.my0);
+  col[TPB] = make_float4(r.my1, r.my2, r.mz0, r.mz1);
+  col[2 * TPB] = make_float4(r.mz2, r.dx, r.dy, r.dz);
+}
+
+template <int TPB, bool PERMUTE>
+struct TriShearSmem {
+  static constexpr bool kPermutePlanes = PERMUTE;
+  const float4 *col;  // this thread's first float4 (shear_column)
+  __device__ __forceinline__ bool operator()(const RayPre &r, float4 v0, float4 v1, float4 v2, float tbest,
+                                             float &t) const {
+    const float4 p = col[0], q = col[TPB], u = col[2 * TPB];
+    const Shear m{p.x, p.y, p.z, p.w, q.x, q.y, q.z, q.w, u.x, u.y, u.z, u.w};
+    return hit_triangle_sheared(r, m, v0, v1, v2, tbest, t);
+  }
+};
+
+template <bool ANY, class Fetch, class Finish, class Tri = TriInRegs>
 __device__ __forceinline__ void trace_dynamic(const SceneView &s, uint32_t n, uint32_t *next, uint2 *stack,
-                                              int stride, int depth, Fetch fetch, Finish finish) {
+                                              int stride, int depth, Fetch fetch, Finish finish, Tri tri = Tri{}) {
   const uint32_t lane = threadIdx.x & 31u;
   RayPre r{};
   float tbest = 0.f;
@@ -419,7 +484,7 @@ __device__ __forceinline__ void trace_dynamic(const SceneView &s, uint32_t n, ui
       continue;  // every lane idle: the next iteration refills the whole warp
     }
     if (active) {
-      if (live) live = trace_step<ANY>(s, r, tbest, best, st, stack, stride, depth);
+      if (live) live = trace_step<ANY>(s, r, tbest, best, st, stack, stride, depth, tri);
       if (!live) {
         finish(idx, best, tbest);
         active = false;

@@ -253,22 +253,20 @@ __device__ __forceinline__ bool regenerate(const Params &prm, const Paths &P, bo
 // scene (eight levels), 960x540 x 16 spp: 26.3 ms static, 23.0 ms dynamic.
 constexpr uint32_t kDynamicDepth = 3;
 
-// Resident blocks of k_extend / k_shadow: one ray per thread (shallow trees) at
-// 1024 / TPB (64 registers at 128 threads; box frame 1.233 -> 1.208 ms); dynamic
-// fetching keeps the compiler's choice (at 1024 / TPB the many-light frame went
-// 0.3037 -> 0.3052 s).
-constexpr int trace_blocks(bool dyn, int tpb) { return dyn || 1024 / tpb < 1 ? 1 : 1024 / tpb; }
-
-// With dynamic fetching the triangle test's ray data (shear rows, direction) sits in
-// shared memory after the stacks (TriShearSmem): k_extend 92 -> 78 registers,
-// k_shadow 89 -> 72 (five -> six and seven CTAs per SM), many-light frame (1080p,
-// 64 spp) 0.332 -> 0.309 s.  Their box test keeps the conversion form: the permute
-// form (80 registers each) ran that frame in 0.318 s.
+// Resident blocks of k_extend / k_shadow: 1024 / TPB, i.e. 64 registers.  One ray
+// per thread (shallow trees): box frame 1.233 -> 1.208 ms against the compiler's
+// choice.  Dynamic fetching (deep trees), where the triangle test's ray data (shear
+// rows, direction) sit in shared memory after the stacks (TriShearSmem): with the
+// rows in registers the kernels took 92 / 89 registers (five CTAs per SM), with them
+// in shared memory 78 / 72 (six / seven CTAs; 1080p 64-spp many-light frame 0.332 ->
+// 0.309 s), and capped at 64 registers without spills, eight CTAs: 0.299 s.  Their
+// box test keeps the conversion form (the permute form at eight CTAs: 0.301 s).
+constexpr int trace_blocks(int tpb) { return 1024 / tpb < 1 ? 1 : 1024 / tpb; }
 
 // Closest hit of the paths in queue `cur`.  DYN: dynamic fetching over the queue,
 // work counter P.counts[3] (zeroed before the launch).
 template <int TPB, bool DYN>
-__global__ void __launch_bounds__(TPB, trace_blocks(DYN, TPB)) k_extend(SceneView s, Paths P, int cur, int depth) {
+__global__ void __launch_bounds__(TPB, trace_blocks(TPB)) k_extend(SceneView s, Paths P, int cur, int depth) {
   extern __shared__ uint2 smem_trav[];
   const uint32_t *q = cur ? P.q1 : P.q0;
   auto fetch = [&](uint32_t i, RayPre &r, float &tmax) {
@@ -301,7 +299,7 @@ __global__ void __launch_bounds__(TPB, trace_blocks(DYN, TPB)) k_extend(SceneVie
 // pixel; occluded ones zero their training record's weight.  DYN: dynamic
 // fetching, work counter P.counts[4] (zeroed before the launch).
 template <int TPB, bool DYN>
-__global__ void __launch_bounds__(TPB, trace_blocks(DYN, TPB)) k_shadow(SceneView s, Paths P, int depth, int cur, float4 *rec) {
+__global__ void __launch_bounds__(TPB, trace_blocks(TPB)) k_shadow(SceneView s, Paths P, int depth, int cur, float4 *rec) {
   extern __shared__ uint2 smem_trav[];
   const uint32_t n = min(P.counts[2], P.sh_cap);
   if (blockIdx.x == 0 && threadIdx.x == 0) {

@@ -61,6 +61,7 @@ struct ShadeView {
 struct ckr_scene {
   int device = 0;
   ckr::DevBuf<float4> nodes, tris, spheres;
+  ckr::DevBuf<uint4> slot_bits;  // per wide node: each slot's hit bits (trace_device.cuh)
   ckr::DevBuf<int> status;
   int32_t root = ckr::kDone;
   uint32_t ntri = 0, nsph = 0, nnodes = 0, nleaves = 0, max_depth = 0, nnodes_binary = 0;

@@ -28,6 +28,7 @@ SceneView view_of(const ckr_scene *s) {
   v.root = s->root;
   v.nsph = s->nsph;
   v.status = s->status.ptr;
+  v.slot_bits = s->slot_bits.ptr;
   return v;
 }
 
@@ -41,8 +42,10 @@ constexpr int kTPB = 128;
 // trace_device.cuh): 64 registers and eight CTAs per SM instead of 72 and seven
 // (closest hit 2.194 -> 2.148 ms per 2^23 rays, any hit 1.621 -> 1.580 ms).  Capping
 // the kernel at 56 or 48 registers (nine or ten CTAs) spilled and was 3 % and 7 %
-// slower.
-constexpr size_t kShearBytes = shear_smem_bytes(kTPB);
+// slower.  After them, the 2 KB octant table of the slot bits (slot_lut): the hit
+// bits of each child come from the scene's slot_bits array (2.145 -> 2.105 ms, any
+// hit 1.576 -> 1.546 ms).
+constexpr size_t kShearBytes = shear_smem_bytes(kTPB) + kSlotLutBytes;
 
 // Closest / any hit over a ray array, with dynamic ray fetching (trace_dynamic).
 template <bool ANY>
@@ -51,6 +54,8 @@ __global__ void __launch_bounds__(kTPB) k_trace_dyn(SceneView s, const float4 *_
                                                     uint8_t *__restrict__ occluded, int depth, uint32_t *next) {
   extern __shared__ uint2 smem_trav[];
   float4 *col = shear_column<kTPB>(smem_trav, depth);
+  const uint8_t *lut = fill_slot_lut<kTPB>(reinterpret_cast<uint8_t *>(col - threadIdx.x + 3 * kTPB));
+  const TriShearSmem<kTPB, true, true> tri_pol{col, lut};
   trace_dynamic<ANY>(
       s, n, next, smem_trav + threadIdx.x, kTPB, depth,
       [&](uint32_t i, RayPre &r, float &tmax) {
@@ -68,7 +73,7 @@ __global__ void __launch_bounds__(kTPB) k_trace_dyn(SceneView s, const float4 *_
           hit_t[i] = t;
         }
       },
-      TriShearSmem<kTPB, true>{col});
+      tri_pol);
 }
 
 struct LaunchShape {
@@ -174,6 +179,19 @@ extern "C" int ckr_scene_create(const float *tri9, uint32_t ntri, const float *s
   if (!bvh.tris.empty() &&
       cudaMemcpy(s->tris.ptr, bvh.tris.data(), bvh.tris.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
     return fail(CKR_ERR_CUDA);
+  {
+    // Each slot's hit bits from its meta byte (pattern << position), interior slots at
+    // 24 + slot (the traversal permutes them for the ray's octant).
+    std::vector<uint32_t> bits(8 * std::max<size_t>(1, bvh.nnodes), 0u);
+    for (size_t n = 0; n < bvh.nnodes; ++n)
+      for (int k = 0; k < 8; ++k) {
+        const uint32_t m = (bvh.nodes[kWideWords * n + 6 + (k >> 2)] >> (8 * (k & 3))) & 0xffu;
+        bits[8 * n + k] = m ? (m >> 5) << (m & 31u) : 0u;
+      }
+    if (s->slot_bits.reserve(bits.size() / 4) != cudaSuccess ||
+        cudaMemcpy(s->slot_bits.ptr, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice) != cudaSuccess)
+      return fail(CKR_ERR_CUDA);
+  }
   if (nsph) {
     s->host_spheres.assign(sph4, sph4 + 4 * (size_t)nsph);
     if (cudaMemcpy(s->spheres.ptr, sph4, 4 * sizeof(float) * nsph, cudaMemcpyHostToDevice) != cudaSuccess)

@@ -27,6 +27,7 @@ struct SceneView {
   int32_t root;           // 0, or kDone when no triangle is indexed
   uint32_t nsph;
   int *status;            // first device error (CKR_ERR_*), 0 when none
+  const uint4 *slot_bits; // per wide node, its eight slots' hit bits (two uint4)
 };
 
 struct RayPre {
@@ -187,10 +188,17 @@ constexpr float kQuantSlack = 2.384185791015625e-07f;
 // registers, spill with the first form and ran 5-10 % slower).  Out:
 // ng = (child_base, hit interior children at bits 24 + (slot ^ oct) | imask),
 // tg = (tri_base, hit triangles at their offsets from tri_base).
-template <bool PERMUTE>
+template <bool PERMUTE, class Tri>
 __device__ __forceinline__ void wide_node(const SceneView &s, const RayPre &r, float tbest, uint32_t node,
-                                          uint2 &ng, uint2 &tg) {
+                                          uint2 &ng, uint2 &tg, const Tri &tri) {
   const float4 *np = s.nodes + 5 * (size_t)node;
+  // With slot bits (Tri::kSlotBits) each slot's hit bits come ready-made from the
+  // scene's slot_bits array instead of being assembled from its meta byte.
+  uint4 cb0 = make_uint4(0, 0, 0, 0), cb1 = cb0;
+  if constexpr (Tri::kSlotBits) {
+    cb0 = __ldg(s.slot_bits + 2 * (size_t)node);
+    cb1 = __ldg(s.slot_bits + 2 * (size_t)node + 1);
+  }
   const float4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
   const uint32_t ei = __float_as_uint(w0.w);
   const float ax = __fmul_rn(__uint_as_float((ei & 0xffu) << 23), r.ix);
@@ -246,8 +254,9 @@ __device__ __forceinline__ void wide_node(const SceneView &s, const RayPre &r, f
   // bit then orders the children front to back for the ray's octant.
   const uint32_t x4 = r.oct * 0x01010101u;
   uint32_t meta[2] = {__float_as_uint(w1.z), __float_as_uint(w1.w)};
+  if constexpr (!Tri::kSlotBits)
 #pragma unroll
-  for (int h = 0; h < 2; ++h) meta[h] ^= (((meta[h] >> 3) & (meta[h] >> 4) & 0x01010101u) * 7u) & x4;
+    for (int h = 0; h < 2; ++h) meta[h] ^= (((meta[h] >> 3) & (meta[h] >> 4) & 0x01010101u) * 7u) & x4;
   uint32_t hits = 0;
 #pragma unroll
   for (int slot = 0; slot < 8; ++slot) {
@@ -266,9 +275,17 @@ __device__ __forceinline__ void wide_node(const SceneView &s, const RayPre &r, f
     // The slot's hit bits: its pattern (bits 5..7 of the meta byte) shifted to its
     // position (bits 0..4).  The funnel shift wraps its shift amount, so the bits
     // above the byte's low five need not be masked off.
+    if constexpr (Tri::kSlotBits) {
+      const uint32_t cw[8] = {cb0.x, cb0.y, cb0.z, cb0.w, cb1.x, cb1.y, cb1.z, cb1.w};
+      if (en <= ex) hits |= cw[slot];
+      continue;
+    }
     const uint32_t m = meta[h] >> sh;
     if (en <= ex) hits |= __funnelshift_l(0u, (m >> 5) & 7u, m);
   }
+  // Slot bits keep interior children at 24 + slot: one table lookup moves them to
+  // 24 + (slot ^ oct) for the ray's octant.
+  if constexpr (Tri::kSlotBits) hits = (hits & 0x00ffffffu) | ((uint32_t)tri.lut[(r.oct << 8) | (hits >> 24)] << 24);
   ng = make_uint2(__float_as_uint(w1.x), (hits & 0xff000000u) | (ei >> 24));
   tg = make_uint2(__float_as_uint(w1.y), hits & 0x00ffffffu);
 }
@@ -302,6 +319,8 @@ __device__ __forceinline__ Trav trav_start(const SceneView &s, const RayPre &r) 
 // from shared memory) and which form of the box test wide_node uses.
 struct TriInRegs {
   static constexpr bool kPermutePlanes = false;
+  static constexpr bool kSlotBits = false;
+  const uint8_t *lut = nullptr;
   __device__ __forceinline__ bool operator()(const RayPre &r, float4 v0, float4 v1, float4 v2, float tbest,
                                              float &t) const {
     return hit_triangle(r, v0, v1, v2, tbest, t);
@@ -336,7 +355,7 @@ __device__ __forceinline__ bool trace_step_rt(const SceneView &s, const RayPre &
           live = false;
         }
       }
-      if (live) wide_node<Tri::kPermutePlanes>(s, r, tbest, child, st.ng, st.tg);
+      if (live) wide_node<Tri::kPermutePlanes>(s, r, tbest, child, st.ng, st.tg, tri);
     }
   }
   if (live && st.tg.y != 0) {
@@ -440,10 +459,31 @@ __device__ __forceinline__ void store_shear(float4 *col, const RayPre &r) {
   col[2 * TPB] = make_float4(r.mz2, r.dx, r.dy, r.dz);
 }
 
-template <int TPB, bool PERMUTE>
+// The octant table of slot bits: lut[oct * 256 + x] has bit s ^ oct set for every
+// bit s of x, so the interior children's hit bits, kept at 24 + slot in the scene's
+// slot_bits, move to 24 + (slot ^ oct) with one shared-memory load per node.  Filled
+// by the block at kernel start (the call ends with a block barrier).
+constexpr size_t kSlotLutBytes = 2048;
+
+template <int TPB>
+__device__ __forceinline__ const uint8_t *fill_slot_lut(uint8_t *lut) {
+  for (uint32_t i = threadIdx.x; i < kSlotLutBytes; i += TPB) {
+    const uint32_t o = i >> 8, x = i & 255u;
+    uint32_t y = 0;
+    for (uint32_t b = 0; b < 8; ++b)
+      if (x >> b & 1u) y |= 1u << (b ^ o);
+    lut[i] = (uint8_t)y;
+  }
+  __syncthreads();
+  return lut;
+}
+
+template <int TPB, bool PERMUTE, bool SLOTBITS = false>
 struct TriShearSmem {
   static constexpr bool kPermutePlanes = PERMUTE;
+  static constexpr bool kSlotBits = SLOTBITS;
   const float4 *col;  // this thread's first float4 (shear_column)
+  const uint8_t *lut = nullptr;
   __device__ __forceinline__ bool operator()(const RayPre &r, float4 v0, float4 v1, float4 v2, float tbest,
                                              float &t) const {
     const float4 p = col[0], q = col[TPB], u = col[2 * TPB];

@@ -185,7 +185,9 @@ constexpr float kQuantSlack = 2.384185791015625e-07f;
 // conversions on the XU pipe: the traversal kernels, 2.27 -> 2.20 ms per 2^23
 // rays); otherwise through an integer-to-float conversion, whose per-node set-up
 // needs fewer registers (the renderer's one-ray-per-thread kernels, capped at 64
-// registers, spill with the first form and ran 5-10 % slower).  Out:
+// registers, spill with the first form and ran 5-10 % slower).  A slot's hit bits
+// are either assembled from its meta byte or, with Tri::kSlotBits (the traversal
+// kernels), read from the scene's slot_bits array.  Out:
 // ng = (child_base, hit interior children at bits 24 + (slot ^ oct) | imask),
 // tg = (tri_base, hit triangles at their offsets from tri_base).
 template <bool PERMUTE, class Tri>
@@ -250,8 +252,8 @@ __device__ __forceinline__ void wide_node(const SceneView &s, const RayPre &r, f
   const uint32_t nx[2] = {sx ? hx0 : lx0, sx ? hx1 : lx1}, fx[2] = {sx ? lx0 : hx0, sx ? lx1 : hx1};
   const uint32_t ny[2] = {sy ? hy0 : ly0, sy ? hy1 : ly1}, fy[2] = {sy ? ly0 : hy0, sy ? ly1 : hy1};
   const uint32_t nz[2] = {sz ? hz0 : lz0, sz ? hz1 : lz1}, fz[2] = {sz ? lz0 : hz0, sz ? lz1 : hz1};
-  // Interior slots' meta bytes (0x38 + slot) become 0x38 + (slot ^ oct): their hit
-  // bit then orders the children front to back for the ray's octant.
+  // Without slot bits, interior slots' meta bytes (0x38 + slot) become 0x38 + (slot ^
+  // oct): their hit bit then orders the children front to back for the ray's octant.
   const uint32_t x4 = r.oct * 0x01010101u;
   uint32_t meta[2] = {__float_as_uint(w1.z), __float_as_uint(w1.w)};
   if constexpr (!Tri::kSlotBits)

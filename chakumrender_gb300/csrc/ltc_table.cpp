@@ -205,3 +205,9 @@ extern "C" int ckr_internal_ltc_shade_host(const float *gbuf, uint32_t npx, cons
   }
   return CKR_OK;
 }
+
+extern "C" int ckr_internal_theta_over_sin_host(const float *c, uint32_t n, float *out) {
+  if (n && (!c || !out)) return CKR_ERR_INVALID_ARGUMENT;
+  for (uint32_t i = 0; i < n; ++i) out[i] = ckr::theta_over_sin(c[i]);
+  return CKR_OK;
+}

@@ -35,6 +35,9 @@ int ckr_internal_brdf_ltc_host(const ckr_material *mats, uint32_t count, const f
 /* LTC polygon-light shading on the host (the device kernel's per-pixel code). */
 int ckr_internal_ltc_shade_host(const float *gbuf, uint32_t npx, const float *light_tri9, const float *light_rgb,
                                 uint32_t nlight, float *rgb);
+/* The edge integral's theta / sin(theta) at theta = acos(c) (the polynomial of
+ * theta_over_sin) on the host, per value. */
+int ckr_internal_theta_over_sin_host(const float *c, uint32_t n, float *out);
 
 /* The network's loss and gradients on n 12-float records in device memory,
  * computed by the tensor-core training kernels without an Adam step. */

@@ -45,7 +45,7 @@ constexpr int kTPB = 128;
 // slower.  After them, the 2 KB octant table of the slot bits (slot_lut): the hit
 // bits of each child come from the scene's slot_bits array (2.145 -> 2.105 ms, any
 // hit 1.576 -> 1.546 ms).
-constexpr size_t kShearBytes = shear_smem_bytes(kTPB) + kSlotLutBytes;
+constexpr size_t kAfterStacksBytes = shear_smem_bytes(kTPB) + kSlotLutBytes;
 
 // Closest / any hit over a ray array, with dynamic ray fetching (trace_dynamic).
 template <bool ANY>
@@ -90,7 +90,7 @@ cudaError_t launch_shape(const ckr_scene *s, LaunchShape &ls) {
   if (e != cudaSuccess) return e;
   e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
-  ls.smem = (size_t)stack_depth_of(s) * kTPB * sizeof(uint2) + kShearBytes;
+  ls.smem = (size_t)stack_depth_of(s) * kTPB * sizeof(uint2) + kAfterStacksBytes;
   if (ls.smem > 48 * 1024) {
     e = cudaFuncSetAttribute(k_trace_dyn<ANY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls.smem);
     if (e != cudaSuccess) return e;
@@ -188,8 +188,9 @@ extern "C" int ckr_scene_create(const float *tri9, uint32_t ntri, const float *s
         const uint32_t m = (bvh.nodes[kWideWords * n + 6 + (k >> 2)] >> (8 * (k & 3))) & 0xffu;
         bits[8 * n + k] = m ? (m >> 5) << (m & 31u) : 0u;
       }
-    if (s->slot_bits.reserve(bits.size() / 4) != cudaSuccess ||
-        cudaMemcpy(s->slot_bits.ptr, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice) != cudaSuccess)
+    if (s->slot_bits.reserve(bits.size() / 4) != cudaSuccess) return fail(CKR_ERR_OUT_OF_MEMORY);
+    if (cudaMemcpy(s->slot_bits.ptr, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice) !=
+        cudaSuccess)
       return fail(CKR_ERR_CUDA);
   }
   if (nsph) {

@@ -142,7 +142,7 @@ __device__ __forceinline__ bool hit_triangle_sheared(const RayPre &r, const Shea
 // root taken above max(tmin, 1e-4).
 __device__ __forceinline__ double hit_sphere(const RayPre &r, float4 s) {
   {
-    // FP32 pre-test (FP64 is slow on this part): a ray whose line passes the sphere
+    // FP32 pre-tests (FP64 is slow on this part).  A ray whose line passes the sphere
     // by more than 1e-5 of the squared magnitudes involved -- orders of magnitude
     // above the FP32 rounding of these few operations -- has a negative FP64
     // discriminant too, so the miss is decided without FP64.  The rounding of b =
@@ -155,7 +155,16 @@ __device__ __forceinline__ double hit_sphere(const RayPre &r, float4 s) {
     const float dd = fmaxf(1.f, r.dx * r.dx + r.dy * r.dy + r.dz * r.dz);
     const float m = fmaxf(fmaxf(fmaxf(fabsf(s.x), fabsf(s.y)), fabsf(s.z)),
                           fmaxf(fmaxf(fabsf(r.ox), fabsf(r.oy)), fabsf(r.oz)));
-    if (b * b - oo + s.w * s.w < -1e-5f * ((m * m + oo) * dd + b * b + s.w * s.w)) return 1e300;
+    const float T = (m * m + oo) * dd + b * b + s.w * s.w;
+    const float det = b * b - oo + s.w * s.w;
+    if (det < -1e-5f * T) return 1e300;
+    // A ray leaving the sphere (bounce and shadow rays from its surface, rays moving
+    // away from it): the far root b + sqrt(det) is below 5e-5 even with b and det
+    // raised by bounds on their FP32 rounding (4e-6 sqrt(T) and 4e-6 T, several times
+    // the few-ulp errors of these sums), so both roots are below the 1e-4 the FP64 test
+    // requires and it would report a miss.  NaN fails the comparison.
+    const float t2u = (b + 4e-6f * sqrtf(T)) + sqrtf(fmaxf(0.f, det + 4e-6f * T));
+    if (t2u < 5e-5f) return 1e300;
   }
   double opx = (double)s.x - r.ox, opy = (double)s.y - r.oy, opz = (double)s.z - r.oz;
   double dx = r.dx, dy = r.dy, dz = r.dz;

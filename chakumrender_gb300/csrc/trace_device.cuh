@@ -140,6 +140,10 @@ __device__ __forceinline__ bool hit_triangle_sheared(const RayPre &r, const Shea
 
 // Sphere::intersect in FP64 (src/geometryPrimitives.cpp:12-27), with the
 // root taken above max(tmin, 1e-4).
+// LEAVING: also the second pre-test, for rays leaving the sphere.  The traversal
+// kernels with dynamic fetching leave it out: their scenes here have no spheres, and
+// the extra code in their refill path cost 0.7 % (many-light frame, A/B).
+template <bool LEAVING = true>
 __device__ __forceinline__ double hit_sphere(const RayPre &r, float4 s) {
   {
     // FP32 pre-tests (FP64 is slow on this part).  A ray whose line passes the sphere
@@ -163,8 +167,10 @@ __device__ __forceinline__ double hit_sphere(const RayPre &r, float4 s) {
     // raised by bounds on their FP32 rounding (4e-6 sqrt(T) and 4e-6 T, several times
     // the few-ulp errors of these sums), so both roots are below the 1e-4 the FP64 test
     // requires and it would report a miss.  NaN fails the comparison.
-    const float t2u = (b + 4e-6f * sqrtf(T)) + sqrtf(fmaxf(0.f, det + 4e-6f * T));
-    if (t2u < 5e-5f) return 1e300;
+    if constexpr (LEAVING) {
+      const float t2u = (b + 4e-6f * sqrtf(T)) + sqrtf(fmaxf(0.f, det + 4e-6f * T));
+      if (t2u < 5e-5f) return 1e300;
+    }
   }
   double opx = (double)s.x - r.ox, opy = (double)s.y - r.oy, opz = (double)s.z - r.oz;
   double dx = r.dx, dy = r.dy, dz = r.dz;
@@ -331,6 +337,7 @@ __device__ __forceinline__ Trav trav_start(const SceneView &s, const RayPre &r) 
 struct TriInRegs {
   static constexpr bool kPermutePlanes = false;
   static constexpr bool kSlotBits = false;
+  static constexpr bool kSphereLeaving = true;
   const uint8_t *lut = nullptr;
   __device__ __forceinline__ bool operator()(const RayPre &r, float4 v0, float4 v1, float4 v2, float tbest,
                                              float &t) const {
@@ -392,10 +399,11 @@ __device__ __forceinline__ bool trace_step(const SceneView &s, const RayPre &r, 
 
 // Spheres of the scene, tested before the triangles.  Returns false when ANY is
 // satisfied by a sphere.
+template <bool LEAVING = true>
 __device__ __forceinline__ bool trace_spheres_rt(const SceneView &s, const RayPre &r, float &tbest, uint32_t &best,
                                                  const bool ANY) {
   for (uint32_t k = 0; k < s.nsph; ++k) {
-    double t = hit_sphere(r, __ldg(&s.spheres[k]));
+    double t = hit_sphere<LEAVING>(r, __ldg(&s.spheres[k]));
     if (t < (double)tbest) {
       tbest = (float)t;
       best = kSphereBit | k;
@@ -493,6 +501,7 @@ template <int TPB, bool PERMUTE, bool SLOTBITS = false>
 struct TriShearSmem {
   static constexpr bool kPermutePlanes = PERMUTE;
   static constexpr bool kSlotBits = SLOTBITS;
+  static constexpr bool kSphereLeaving = false;
   const float4 *col;  // this thread's first float4 (shear_column)
   const uint8_t *lut = nullptr;
   __device__ __forceinline__ bool operator()(const RayPre &r, float4 v0, float4 v1, float4 v2, float tbest,
@@ -525,7 +534,7 @@ __device__ __forceinline__ void trace_dynamic(const SceneView &s, uint32_t n, ui
         if (idx < n && fetch(idx, r, tbest)) {
           best = kMiss;
           st = trav_start(s, r);
-          live = trace_spheres<ANY>(s, r, tbest, best);
+          live = trace_spheres_rt<Tri::kSphereLeaving>(s, r, tbest, best, ANY);
           active = true;
         }
       }
